@@ -1,0 +1,150 @@
+/* openpiv_gb300.h -- C ABI of the GB300 (sm_103a) PIV window-correlation path.
+ *
+ * Drop-in for the per-window hot loop of OpenPIV-c++ (examples/process/
+ * main.cpp:189-237): every interrogation window of an image pair is
+ * extracted, correlated (FFT::cross_correlate or FFT::cross_correlate_real),
+ * peak-searched (core::find_peaks, 2 peaks, radius 1), Gaussian-fitted
+ * (core::fit_simple_gaussian) and turned into a vector {x, y, u, v, sn}
+ * exactly as that loop does, by hand-written CUDA kernels on one GPU.
+ *
+ * Plain C: pointers, sizes and status codes only.  The caller owns every
+ * buffer passed in; a plan owns its device scratch.  No function keeps a
+ * pointer passed to it after it returns, except where a stream is given
+ * (the device-buffer calls are asynchronous on that stream).
+ *
+ * Status codes mirror the exceptions the reference throws; the message of
+ * the last failure on the calling thread is returned by opiv_last_error().
+ */
+#ifndef OPENPIV_GB300_H
+#define OPENPIV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+    OPIV_OK = 0,
+    OPIV_ERR_OFFSET_RANGE = -1,   /* "offsets must be between 0.0 and 1.0"      grid.impl.h:14-15 */
+    OPIV_ERR_IMAGE_EMPTY = -2,    /* "image size must be non-zero"              grid.impl.h:29-30 */
+    OPIV_ERR_IA_EMPTY = -3,       /* "interrogation size must be non-zero"      grid.impl.h:32-33 */
+    OPIV_ERR_OFFSET_ZERO = -4,    /* "offsets must be non-zero"                 grid.impl.h:35-36 */
+    OPIV_ERR_IA_TOO_BIG = -5,     /* "interrogation size is bigger than image"  grid.impl.h:38-40 */
+    OPIV_ERR_NOT_POW2 = -6,       /* "dimensions must be power of 2"            fft.h:81-83 */
+    OPIV_ERR_CAPACITY = -7,       /* output buffer too small */
+    OPIV_ERR_RECT_OUTSIDE = -8,   /* "extract: rectangle to extract is too large for image"
+                                     image_utils.impl.h:396-401 */
+    OPIV_ERR_ARG = -9,            /* invalid argument (null pointer, bad enum) */
+    OPIV_ERR_SIZE_MISMATCH = -10, /* "image size is different from expected"    fft.h:94-98, :136-141 */
+    OPIV_ERR_UNSUPPORTED = -11,   /* window size this build has no kernel for */
+    OPIV_ERR_CUDA = -12,          /* a CUDA runtime call failed */
+    OPIV_ERR_NO_DEVICE = -13      /* no CUDA device */
+};
+
+/* ---- enums -------------------------------------------------------------- */
+enum { OPIV_U8 = 0, OPIV_U16 = 1, OPIV_F32 = 2 };           /* pixel type of the frames */
+enum { OPIV_CORR_REAL = 0,      /* FFT::cross_correlate_real, fft.h:208-227 (spectrum row 0,
+                                   row H/2 and column 0 left at zero, as the reference does) */
+       OPIV_CORR_COMPLEX = 1 }; /* FFT::cross_correlate, fft.h:188-206 (circular correlation) */
+
+/* Per-window result, as the reference's point_vector (main.cpp:144-149):
+ * x, y   window midpoint, y measured from the image top (H - y, main.cpp:230)
+ * u, v   midpoint - (bottom-left + fitted peak)        (main.cpp:227)
+ * sn     first peak / second peak if the second is > 0 (main.cpp:233-234)
+ * All five are 0 when fewer than two peaks were found (main.cpp:214-218). */
+typedef struct { float x, y, u, v, sn; } opiv_vector;
+
+/* peak code per window: py * W + px of the first peak in the quadrant-
+ * swapped plane (zero lag at (W/2, W/2)), or -1 when fewer than two peaks;
+ * OPIV_PEAK_EXACT is or-ed in when the window was decided by the exact
+ * double-precision pass rather than the FP32 pass. */
+#define OPIV_PEAK_EXACT 0x40000000
+#define OPIV_PEAK_MASK 0x0000FFFF
+
+typedef struct opiv_plan opiv_plan;
+
+/* ---- library ------------------------------------------------------------ */
+const char* opiv_last_error(void);
+const char* opiv_status_string(int status);
+int opiv_version(void);
+/* number of GPU kernel launches issued by this thread's calls so far */
+int64_t opiv_kernel_launch_count(void);
+
+/* ---- grid (host; bit-exact with the reference) --------------------------- */
+/* core::generate_cartesian_grid(size, size, double)  grid.h:88-91, grid.impl.h:9-22.
+ * Writes (x, y) bottom-left corners, y outer / x inner.  out_xy may be NULL
+ * to query the count.  Returns the window count or a negative status. */
+int64_t opiv_grid(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_t ia_h,
+                  double step_fraction, int32_t* out_xy, int64_t cap);
+/* core::generate_cartesian_grid(size, size, array<uint32_t,2>)  grid.h:104-107,
+ * grid.impl.h:24-61. */
+int64_t opiv_grid_offsets(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_t ia_h,
+                          uint32_t dx, uint32_t dy, int32_t* out_xy, int64_t cap);
+
+/* ---- plans -------------------------------------------------------------- */
+/* A plan fixes image size, pixel type, window size, grid step and mode, and
+ * owns the device scratch for one pair at a time.  ia must be a power of two
+ * the build has a kernel for (16, 32 or 64): fft.h:76-84 throws for non-powers
+ * of two (OPIV_ERR_NOT_POW2); other powers of two give OPIV_ERR_UNSUPPORTED.
+ * dx, dy: grid step in pixels (generate_cartesian_grid's offsets).
+ * limit_search: search peaks only in the centre rect().dilate(0.5) of the
+ * plane (main.cpp:204-208). */
+int opiv_plan_create(opiv_plan** plan, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
+                     uint32_t dx, uint32_t dy, int mode, int limit_search, int device);
+int opiv_plan_destroy(opiv_plan* plan);
+int64_t opiv_plan_window_count(const opiv_plan* plan);
+/* copies the plan's grid (bottom-left corners) to out_xy (2 * count int32) */
+int opiv_plan_grid(const opiv_plan* plan, int32_t* out_xy, int64_t cap);
+
+/* Whole pass over one image pair, host buffers in and out (synchronous).
+ * frame_a, frame_b: img_h rows of pitch_bytes each.  out_vec: count
+ * entries.  out_peak: count int32 or NULL.  Replaces the grid loop of
+ * main.cpp:239-302 (with the processor of :189-237). */
+int opiv_process_pair(opiv_plan* plan, const void* frame_a, const void* frame_b, size_t pitch_bytes,
+                      opiv_vector* out_vec, int32_t* out_peak);
+
+/* Same, all buffers on the device, asynchronous on `stream` (a cudaStream_t;
+ * NULL = legacy default stream).  d_out_peak may be NULL. */
+int opiv_process_pair_device(opiv_plan* plan, const void* d_frame_a, const void* d_frame_b,
+                             size_t pitch_bytes, opiv_vector* d_out_vec, int32_t* d_out_peak,
+                             void* stream);
+
+/* number of windows the last pass sent to the exact double-precision
+ * re-evaluation (synchronises with the plan's last pass) */
+int64_t opiv_plan_exact_count(opiv_plan* plan);
+
+/* Kernel timing, the GPU counterpart of the reference's "processing time"
+ * log (main.cpp:239, :304-309).  When enabled, every pass records CUDA
+ * events around its two kernels on the pass's stream; opiv_plan_last_timing
+ * waits for the last pass and returns the FP32 kernel's and the exact
+ * pass's durations in milliseconds. */
+int opiv_plan_set_timing(opiv_plan* plan, int enable);
+int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
+
+/* ---- per-window correlation (FFT::cross_correlate[_real] on a batch) ------ */
+/* n window pairs of w x w doubles (a, b: n*w*w each, row-major), planes out:
+ * n*w*w doubles, quadrant-swapped as the reference returns them.
+ * exact = 0: FP32 kernels + exact pedestal (within 1e-5 of the plane peak);
+ * exact = 1: double-precision kernels that repeat the reference's arithmetic
+ * operation for operation (bit-identical planes).  Host buffers, synchronous.
+ * FFT::cross_correlate / cross_correlate_real: fft.h:188-227. */
+int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int64_t n, int mode,
+                               int exact, double* out_planes, int device);
+
+/* ---- host helpers of the same path (no GPU) ------------------------------ */
+/* core::find_peaks(im, num_peaks, radius): image_utils.impl.h:42-74.  Writes
+ * up to num_peaks centres (x, y) and values, highest first; returns count. */
+int opiv_find_peaks(const double* im, uint32_t w, uint32_t h, uint16_t num_peaks, uint32_t radius,
+                    int32_t* out_xy, double* out_value);
+/* core::fit_simple_gaussian on the 3x3 around (px, py): image_utils.impl.h:77-101 */
+int opiv_fit_simple_gaussian(const double* plane, uint32_t w, uint32_t h, int32_t px, int32_t py,
+                             double* out_xy);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENPIV_GB300_H */

@@ -1,0 +1,575 @@
+// opiv_api.cpp -- the C ABI (include/openpiv_gb300.h): validation, grids,
+// plans, device buffers and kernel launches.  Host C++17; the kernels are in
+// piv_fp32_w*.cu and piv_exact.cu.
+//
+// Errors: every entry point returns a status code; the message of the last
+// failure on the calling thread is kept for opiv_last_error().  Messages
+// start with the same text as the exceptions the reference throws.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "openpiv_gb300.h"
+#include "piv_kernels.h"
+
+using namespace opiv;
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local int64_t g_launches = 0;
+
+int fail(int status, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    return fail(OPIV_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(call)                                          \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);     \
+    } while (0)
+
+// openpiv/core/util.h:67-70
+bool is_pow2(uint64_t v) { return v && (v == (v & (~v + 1))); }
+
+size_t px_bytes(int dtype)
+{
+    switch (dtype) {
+    case OPIV_U8: return 1;
+    case OPIV_U16: return 2;
+    case OPIV_F32: return 4;
+    default: return 0;
+    }
+}
+
+struct grid_geom {
+    int64_t xc = 0, yc = 0;
+    int64_t xs = 0, ys = 0;
+};
+
+// generate_cartesian_grid(size, size, array<uint32_t,2>) argument checks and
+// geometry: openpiv/core/detail/grid.impl.h:29-48 (same unsigned arithmetic).
+int grid_geometry(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_t ia_h, uint32_t dx,
+                  uint32_t dy, grid_geom& g)
+{
+    if ((uint64_t)img_w * img_h == 0) return fail(OPIV_ERR_IMAGE_EMPTY, "image size must be non-zero");
+    if ((uint64_t)ia_w * ia_h == 0)
+        return fail(OPIV_ERR_IA_EMPTY, "interrogation size must be non-zero");
+    if (dx == 0 || dy == 0) return fail(OPIV_ERR_OFFSET_ZERO, "offsets must be non-zero");
+    if (ia_w > img_w || ia_h > img_h)
+        return fail(OPIV_ERR_IA_TOO_BIG, "interrogation size is bigger than image");
+    const uint32_t xc = 1 + (img_w - ia_w) / dx;
+    const uint32_t yc = 1 + (img_h - ia_h) / dy;
+    g.xc = xc;
+    g.yc = yc;
+    g.xs = (img_w - ia_w - (dx * (xc - 1))) / 2;
+    g.ys = (img_h - ia_h - (dy * (yc - 1))) / 2;
+    return OPIV_OK;
+}
+
+// Twiddle table exactly as the reference builds it (fft.h:274-294):
+// entry i = (cos t, sin t), t = (s * M_PI * i) / n, s = -1 forward, +1 reverse.
+std::vector<double2> reference_twiddles(uint32_t n, int dir)
+{
+    std::vector<double2> t(n);
+    const double s = dir < 0 ? -1.0 : 1.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const double theta = (s * M_PI * (double)(int)i) / (double)n;
+        t[i] = make_double2(std::cos(theta), std::sin(theta));
+    }
+    return t;
+}
+
+constexpr int kExactBlocks = 152 * 2;   // CTAs of the exact pass (two per SM)
+
+}  // namespace
+
+struct opiv_plan {
+    int device = 0;
+    uint32_t img_w = 0, img_h = 0, ia = 0, dx = 0, dy = 0;
+    int dtype = 0, mode = 0, limit = 0;
+    grid_geom g;
+    int64_t n_win = 0;
+    cudaStream_t stream = nullptr;      // used by the host-buffer calls
+    void* d_fa = nullptr;               // frames for the host-buffer calls
+    void* d_fb = nullptr;
+    size_t d_pitch = 0;
+    opiv_vector* d_vec = nullptr;
+    int32_t* d_peak = nullptr;
+    unsigned int* d_flag_count = nullptr;
+    int32_t* d_flag_list = nullptr;
+    double2* d_tw = nullptr;            // forward then reverse, ia entries each
+    unsigned int* h_flag_count = nullptr;   // pinned copy of the last count
+    bool timing = false;
+    cudaEvent_t ev[3] = { nullptr, nullptr, nullptr };   // fp32 start, fp32 end, exact end
+};
+
+namespace {
+
+void plan_free(opiv_plan* p)
+{
+    if (!p) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    cudaFree(p->d_fa);
+    cudaFree(p->d_fb);
+    cudaFree(p->d_vec);
+    cudaFree(p->d_peak);
+    cudaFree(p->d_flag_count);
+    cudaFree(p->d_flag_list);
+    cudaFree(p->d_tw);
+    if (p->h_flag_count) cudaFreeHost(p->h_flag_count);
+    for (cudaEvent_t& e : p->ev)
+        if (e) cudaEventDestroy(e);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    cudaSetDevice(prev);
+    delete p;
+}
+
+PivParams base_params(const opiv_plan* p)
+{
+    PivParams k;
+    k.img_w = (int)p->img_w;
+    k.img_h = (int)p->img_h;
+    k.gx0 = (int)p->g.xs;
+    k.gy0 = (int)p->g.ys;
+    k.gdx = (int)p->dx;
+    k.gdy = (int)p->dy;
+    k.gnx = (int)p->g.xc;
+    k.n_win = p->n_win;
+    k.flag_count = p->d_flag_count;
+    k.flag_list = p->d_flag_list;
+    k.tw_fwd = p->d_tw;
+    k.tw_rev = p->d_tw + p->ia;
+    return k;
+}
+
+// One pass: FP32 kernel over all windows, then the exact pass over the
+// flagged ones.  Two kernel launches.
+int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_vector* vec,
+             int32_t* peak, cudaStream_t s)
+{
+    PivParams k = base_params(p);
+    k.fa = fa;
+    k.fb = fb;
+    k.pitch = pitch;
+    k.out_vec = vec;
+    k.out_peak = peak;
+    CUDA_TRY(cudaMemsetAsync(p->d_flag_count, 0, sizeof(unsigned int), s));
+    if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
+    CUDA_TRY(launch_piv_fp32(k, (int)p->ia, p->dtype, p->mode, p->limit, false, s));
+    ++g_launches;
+    if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[1], s));
+    CUDA_TRY(launch_piv_exact(k, (int)p->ia, p->dtype, p->mode, p->limit, true, kExactBlocks, s));
+    ++g_launches;
+    if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[2], s));
+    return OPIV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* opiv_last_error(void) { return g_last_error.c_str(); }
+
+const char* opiv_status_string(int s)
+{
+    switch (s) {
+    case OPIV_OK: return "ok";
+    case OPIV_ERR_OFFSET_RANGE: return "offsets must be between 0.0 and 1.0";
+    case OPIV_ERR_IMAGE_EMPTY: return "image size must be non-zero";
+    case OPIV_ERR_IA_EMPTY: return "interrogation size must be non-zero";
+    case OPIV_ERR_OFFSET_ZERO: return "offsets must be non-zero";
+    case OPIV_ERR_IA_TOO_BIG: return "interrogation size is bigger than image";
+    case OPIV_ERR_NOT_POW2: return "dimensions must be power of 2";
+    case OPIV_ERR_CAPACITY: return "output buffer too small";
+    case OPIV_ERR_RECT_OUTSIDE: return "extract: rectangle to extract is too large for image";
+    case OPIV_ERR_ARG: return "invalid argument";
+    case OPIV_ERR_SIZE_MISMATCH: return "image size is different from expected";
+    case OPIV_ERR_UNSUPPORTED: return "unsupported window size";
+    case OPIV_ERR_CUDA: return "CUDA error";
+    case OPIV_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+int opiv_version(void) { return 100; }
+
+int64_t opiv_kernel_launch_count(void) { return g_launches; }
+
+int64_t opiv_grid_offsets(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_t ia_h,
+                          uint32_t dx, uint32_t dy, int32_t* out_xy, int64_t cap)
+{
+    grid_geom g;
+    const int rc = grid_geometry(img_w, img_h, ia_w, ia_h, dx, dy, g);
+    if (rc != OPIV_OK) return rc;
+    const int64_t n = g.xc * g.yc;
+    if (out_xy == nullptr) return n;
+    if (cap < n) return fail(OPIV_ERR_CAPACITY, "grid needs %lld entries, buffer has %lld",
+                             (long long)n, (long long)cap);
+    int64_t k = 0;
+    for (int64_t y = 0; y < g.yc; ++y)
+        for (int64_t x = 0; x < g.xc; ++x, ++k) {
+            out_xy[2 * k] = (int32_t)(g.xs + x * dx);
+            out_xy[2 * k + 1] = (int32_t)(g.ys + y * dy);
+        }
+    return n;
+}
+
+int64_t opiv_grid(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_t ia_h,
+                  double step_fraction, int32_t* out_xy, int64_t cap)
+{
+    // grid.impl.h:14-21
+    if (step_fraction < 0.0 || step_fraction > 1.0)
+        return fail(OPIV_ERR_OFFSET_RANGE, "offsets must be between 0.0 and 1.0");
+    return opiv_grid_offsets(img_w, img_h, ia_w, ia_h, (uint32_t)(ia_w * step_fraction),
+                             (uint32_t)(ia_h * step_fraction), out_xy, cap);
+}
+
+int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
+                     uint32_t dx, uint32_t dy, int mode, int limit_search, int device)
+{
+    if (out == nullptr) return fail(OPIV_ERR_ARG, "plan pointer is null");
+    *out = nullptr;
+    if (px_bytes(dtype) == 0) return fail(OPIV_ERR_ARG, "unknown pixel type %d", dtype);
+    if (mode != OPIV_CORR_REAL && mode != OPIV_CORR_COMPLEX)
+        return fail(OPIV_ERR_ARG, "unknown correlation mode %d", mode);
+    grid_geom g;
+    int rc = grid_geometry(img_w, img_h, ia, ia, dx, dy, g);
+    if (rc != OPIV_OK) return rc;
+    if (!is_pow2(ia)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", ia, ia);
+    if (!fp32_supports((int)ia) || !exact_supports((int)ia))
+        return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", ia, ia);
+    if (g.xs + (int64_t)dx * (g.xc - 1) + ia > (int64_t)img_w || g.ys + (int64_t)dy * (g.yc - 1) + ia > (int64_t)img_h)
+        return fail(OPIV_ERR_RECT_OUTSIDE, "extract: rectangle to extract is too large for image");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(OPIV_ERR_NO_DEVICE, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(OPIV_ERR_ARG, "device %d out of range", device);
+
+    opiv_plan* p = new (std::nothrow) opiv_plan;
+    if (!p) return fail(OPIV_ERR_ARG, "out of host memory");
+    p->device = device;
+    p->img_w = img_w;
+    p->img_h = img_h;
+    p->ia = ia;
+    p->dx = dx;
+    p->dy = dy;
+    p->dtype = dtype;
+    p->mode = mode;
+    p->limit = limit_search ? 1 : 0;
+    p->g = g;
+    p->n_win = g.xc * g.yc;
+
+    int prev = 0;
+    cudaGetDevice(&prev);
+    auto done = [&](int status) {
+        cudaSetDevice(prev);
+        if (status != OPIV_OK) plan_free(p);
+        else *out = p;
+        return status;
+    };
+    cudaError_t e;
+    if ((e = cudaSetDevice(device)) != cudaSuccess) return done(cuda_fail(e, "cudaSetDevice"));
+    if ((e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaStreamCreate"));
+    if ((e = cudaMalloc(&p->d_vec, sizeof(opiv_vector) * p->n_win)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMalloc(vectors)"));
+    if ((e = cudaMalloc(&p->d_peak, sizeof(int32_t) * p->n_win)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMalloc(peaks)"));
+    if ((e = cudaMalloc(&p->d_flag_count, sizeof(unsigned int))) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMalloc(flag count)"));
+    if ((e = cudaMalloc(&p->d_flag_list, sizeof(int32_t) * p->n_win)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMalloc(flag list)"));
+    if ((e = cudaMemset(p->d_flag_count, 0, sizeof(unsigned int))) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemset"));
+    if ((e = cudaMallocHost(&p->h_flag_count, sizeof(unsigned int))) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMallocHost"));
+    *p->h_flag_count = 0;
+    std::vector<double2> tw = reference_twiddles(ia, -1), tr = reference_twiddles(ia, +1);
+    tw.insert(tw.end(), tr.begin(), tr.end());
+    if ((e = cudaMalloc(&p->d_tw, sizeof(double2) * tw.size())) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMalloc(twiddles)"));
+    if ((e = cudaMemcpy(p->d_tw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy(twiddles)"));
+    return done(OPIV_OK);
+}
+
+int opiv_plan_destroy(opiv_plan* plan)
+{
+    plan_free(plan);
+    return OPIV_OK;
+}
+
+int64_t opiv_plan_window_count(const opiv_plan* plan)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    return plan->n_win;
+}
+
+int opiv_plan_grid(const opiv_plan* plan, int32_t* out_xy, int64_t cap)
+{
+    if (!plan || !out_xy) return fail(OPIV_ERR_ARG, "null argument");
+    const int64_t n = opiv_grid_offsets(plan->img_w, plan->img_h, plan->ia, plan->ia, plan->dx,
+                                        plan->dy, out_xy, cap);
+    return n < 0 ? (int)n : OPIV_OK;
+}
+
+int opiv_process_pair_device(opiv_plan* plan, const void* d_fa, const void* d_fb,
+                             size_t pitch_bytes, opiv_vector* d_out_vec, int32_t* d_out_peak,
+                             void* stream)
+{
+    if (!plan || !d_fa || !d_fb || !d_out_vec) return fail(OPIV_ERR_ARG, "null argument");
+    if (pitch_bytes < (size_t)plan->img_w * px_bytes(plan->dtype) ||
+        pitch_bytes % px_bytes(plan->dtype) != 0)
+        return fail(OPIV_ERR_ARG, "pitch %zu too small or not a multiple of the pixel size",
+                    pitch_bytes);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(plan->device);
+    const int rc = run_pass(plan, d_fa, d_fb, pitch_bytes, d_out_vec, d_out_peak,
+                            (cudaStream_t)stream);
+    if (rc == OPIV_OK)
+        cudaMemcpyAsync(plan->h_flag_count, plan->d_flag_count, sizeof(unsigned int),
+                        cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int opiv_process_pair(opiv_plan* plan, const void* frame_a, const void* frame_b, size_t pitch_bytes,
+                      opiv_vector* out_vec, int32_t* out_peak)
+{
+    if (!plan || !frame_a || !frame_b || !out_vec) return fail(OPIV_ERR_ARG, "null argument");
+    const size_t row = (size_t)plan->img_w * px_bytes(plan->dtype);
+    if (pitch_bytes < row) return fail(OPIV_ERR_ARG, "pitch %zu smaller than a row", pitch_bytes);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(plan->device);
+    auto done = [&](int s) { cudaSetDevice(prev); return s; };
+    cudaError_t e;
+    if (!plan->d_fa) {
+        if ((e = cudaMalloc(&plan->d_fa, row * plan->img_h)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaMalloc(frame)"));
+        if ((e = cudaMalloc(&plan->d_fb, row * plan->img_h)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaMalloc(frame)"));
+        plan->d_pitch = row;
+    }
+    cudaStream_t s = plan->stream;
+    if ((e = cudaMemcpy2DAsync(plan->d_fa, plan->d_pitch, frame_a, pitch_bytes, row, plan->img_h,
+                               cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy2DAsync(frame a)"));
+    if ((e = cudaMemcpy2DAsync(plan->d_fb, plan->d_pitch, frame_b, pitch_bytes, row, plan->img_h,
+                               cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy2DAsync(frame b)"));
+    int rc = run_pass(plan, plan->d_fa, plan->d_fb, plan->d_pitch, plan->d_vec,
+                      out_peak ? plan->d_peak : nullptr, s);
+    if (rc != OPIV_OK) return done(rc);
+    if ((e = cudaMemcpyAsync(out_vec, plan->d_vec, sizeof(opiv_vector) * plan->n_win,
+                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpyAsync(vectors)"));
+    if (out_peak &&
+        (e = cudaMemcpyAsync(out_peak, plan->d_peak, sizeof(int32_t) * plan->n_win,
+                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpyAsync(peaks)"));
+    cudaMemcpyAsync(plan->h_flag_count, plan->d_flag_count, sizeof(unsigned int),
+                    cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaStreamSynchronize"));
+    return done(OPIV_OK);
+}
+
+int64_t opiv_plan_exact_count(opiv_plan* plan)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    cudaDeviceSynchronize();
+    return (int64_t)*plan->h_flag_count;
+}
+
+int opiv_plan_set_timing(opiv_plan* plan, int enable)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    if (enable && !plan->ev[0]) {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(plan->device);
+        for (cudaEvent_t& e : plan->ev) {
+            const cudaError_t r = cudaEventCreate(&e);
+            if (r != cudaSuccess) {
+                cudaSetDevice(prev);
+                return cuda_fail(r, "cudaEventCreate");
+            }
+        }
+        cudaSetDevice(prev);
+    }
+    plan->timing = enable != 0;
+    return OPIV_OK;
+}
+
+int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms)
+{
+    if (!plan || !fp32_ms || !exact_ms) return fail(OPIV_ERR_ARG, "null argument");
+    if (!plan->timing) return fail(OPIV_ERR_ARG, "timing is not enabled on this plan");
+    CUDA_TRY(cudaEventSynchronize(plan->ev[2]));
+    CUDA_TRY(cudaEventElapsedTime(fp32_ms, plan->ev[0], plan->ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(exact_ms, plan->ev[1], plan->ev[2]));
+    return OPIV_OK;
+}
+
+int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int64_t n, int mode,
+                               int exact, double* out_planes, int device)
+{
+    if (!a || !b || !out_planes || n < 0) return fail(OPIV_ERR_ARG, "null argument");
+    if (mode != OPIV_CORR_REAL && mode != OPIV_CORR_COMPLEX)
+        return fail(OPIV_ERR_ARG, "unknown correlation mode %d", mode);
+    if (!is_pow2(w)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", w, w);
+    if (exact ? !exact_supports((int)w) : !fp32_supports((int)w))
+        return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", w, w);
+    if (n == 0) return OPIV_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) return fail(OPIV_ERR_NO_DEVICE, "cannot use device %d", device);
+    const size_t N = (size_t)w * w;
+    // The windows are stacked into one w x (n*w) double "frame"; window k
+    // sits at (0, k*w).
+    double *d_a = nullptr, *d_b = nullptr, *d_pl64 = nullptr, *d_peds = nullptr;
+    float* d_pl = nullptr;
+    int32_t* d_xy = nullptr;
+    opiv_vector* d_vec = nullptr;
+    double2* d_tw = nullptr;
+    std::vector<int32_t> xy(2 * n);
+    for (int64_t k = 0; k < n; ++k) { xy[2 * k] = 0; xy[2 * k + 1] = (int32_t)(k * w); }
+    int rc = OPIV_OK;
+    cudaError_t e = cudaSuccess;
+    do {
+        if ((e = cudaMalloc(&d_a, sizeof(double) * N * n)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&d_b, sizeof(double) * N * n)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&d_xy, sizeof(int32_t) * 2 * n)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&d_vec, sizeof(opiv_vector) * n)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d_a, a, sizeof(double) * N * n, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d_b, b, sizeof(double) * N * n, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d_xy, xy.data(), sizeof(int32_t) * 2 * n, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        PivParams k;
+        k.fa = d_a;
+        k.fb = d_b;
+        k.pitch = sizeof(double) * w;
+        k.img_w = (int)w;
+        k.img_h = (int)(w * n);
+        k.win_xy = d_xy;
+        k.n_win = n;
+        k.out_vec = d_vec;
+        if (exact) {
+            std::vector<double2> tw = reference_twiddles(w, -1), tr = reference_twiddles(w, +1);
+            tw.insert(tw.end(), tr.begin(), tr.end());
+            if ((e = cudaMalloc(&d_tw, sizeof(double2) * tw.size())) != cudaSuccess) break;
+            if ((e = cudaMemcpy(d_tw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&d_pl64, sizeof(double) * N * n)) != cudaSuccess) break;
+            k.tw_fwd = d_tw;
+            k.tw_rev = d_tw + w;
+            k.planes64 = d_pl64;
+            const int blocks = (int)std::min<int64_t>(n, 4096);
+            if ((e = launch_piv_exact(k, (int)w, kF64, mode, 0, false, blocks, nullptr)) != cudaSuccess) break;
+            ++g_launches;
+            if ((e = cudaMemcpy(out_planes, d_pl64, sizeof(double) * N * n, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+        } else {
+            if ((e = cudaMalloc(&d_pl, sizeof(float) * N * n)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&d_peds, sizeof(double) * n)) != cudaSuccess) break;
+            k.planes = d_pl;
+            k.peds = d_peds;
+            if ((e = launch_piv_fp32(k, (int)w, kF64, mode, 0, true, nullptr)) != cudaSuccess) break;
+            ++g_launches;
+            std::vector<float> pl(N * n);
+            std::vector<double> peds(n);
+            if ((e = cudaMemcpy(pl.data(), d_pl, sizeof(float) * N * n, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+            if ((e = cudaMemcpy(peds.data(), d_peds, sizeof(double) * n, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+            for (int64_t q = 0; q < n; ++q)
+                for (size_t i = 0; i < N; ++i)
+                    out_planes[q * N + i] = (double)pl[q * N + i] + peds[q];
+        }
+        e = cudaDeviceSynchronize();
+    } while (0);
+    if (e != cudaSuccess) rc = cuda_fail(e, "opiv_cross_correlate_batch");
+    cudaFree(d_a);
+    cudaFree(d_b);
+    cudaFree(d_pl64);
+    cudaFree(d_peds);
+    cudaFree(d_pl);
+    cudaFree(d_xy);
+    cudaFree(d_vec);
+    cudaFree(d_tw);
+    cudaSetDevice(prev);
+    return rc;
+}
+
+// core::find_peaks, image_utils.impl.h:42-74 (host).  The sort is the
+// reference's: std::sort, descending by centre value.
+int opiv_find_peaks(const double* im, uint32_t w, uint32_t h, uint16_t num_peaks, uint32_t r,
+                    int32_t* out_xy, double* out_value)
+{
+    if (!im || !out_xy || !out_value) return fail(OPIV_ERR_ARG, "null argument");
+    struct pk { double v; int32_t x, y; };
+    std::vector<pk> res;
+    for (uint32_t y = r; y < h - 2 * r; ++y) {
+        const double* above = im + (size_t)(y - 1) * w;
+        const double* line = im + (size_t)y * w;
+        const double* below = im + (size_t)(y + 1) * w;
+        for (uint32_t x = r; x < w - r; ++x)
+            if (line[x - 1] < line[x] && line[x + 1] < line[x] && above[x] < line[x] &&
+                below[x] < line[x])
+                res.push_back(pk{ line[x], (int32_t)x, (int32_t)y });
+    }
+    std::sort(res.begin(), res.end(), [](const pk& p, const pk& q) { return p.v > q.v; });
+    const size_t n = std::min(res.size(), (size_t)num_peaks);
+    for (size_t i = 0; i < n; ++i) {
+        out_xy[2 * i] = res[i].x;
+        out_xy[2 * i + 1] = res[i].y;
+        out_value[i] = res[i].v;
+    }
+    return (int)n;
+}
+
+// core::fit_simple_gaussian on the 3x3 view centred at (px, py):
+// image_utils.impl.h:77-101 (host).
+int opiv_fit_simple_gaussian(const double* plane, uint32_t w, uint32_t h, int32_t px, int32_t py,
+                             double* out_xy)
+{
+    if (!plane || !out_xy) return fail(OPIV_ERR_ARG, "null argument");
+    if (px < 1 || py < 1 || (uint32_t)px + 1 >= w || (uint32_t)py + 1 >= h)
+        return fail(OPIV_ERR_ARG, "fit_simple_gaussian: input must be 3x3");
+    auto f = [](double l, double c, double r) {
+        const double num = std::log(l) - std::log(r);
+        const double den = 2.0 * (std::log(l) + std::log(r) - 2.0 * std::log(c));
+        if (den == 0.0) return 0.0;
+        return num / den;
+    };
+    const double* row = plane + (size_t)py * w;
+    out_xy[0] = (double)px + f(row[px - 1], row[px], row[px + 1]);
+    out_xy[1] = (double)py + f(plane[(size_t)(py - 1) * w + px], row[px], plane[(size_t)(py + 1) * w + px]);
+    return OPIV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,307 @@
+// piv_exact.cu -- exact double-precision window kernel for sm_103a.
+//
+// Repeats the reference's double arithmetic operation for operation, so its
+// correlation planes are bit-identical to OpenPIV-c++ built without fused
+// multiply-add contraction:
+//   * 2-D FFT = radix-2 DIT on every row, then every column (fft.h:87-119),
+//     with the same butterfly graph as the recursive fft_inner
+//     (fft.h:245-263): e + o*w, e - o*w, w = table[k * 2n/len], where the
+//     table entries exp(-+i*pi*j/n) are computed on the host with the
+//     reference's own expression (fft.h:274-294);
+//   * complex product (a*c - b*d, b*c + a*d) (pixel_types.h:159-163), every
+//     multiply and add rounded separately (__dmul_rn / __dadd_rn, no FMA);
+//   * REAL mode: the partial two-for-one unpack of fft.h:163-183;
+//   * swap_quadrants (image_utils.impl.h:367-386) as an index remap;
+//   * find_peaks (image_utils.impl.h:42-74) with exact comparisons; among
+//     equal values the first peak is the one std::sort puts first (its
+//     introsort is replayed, sort_order.h);
+//   * fit_simple_gaussian (impl:77-101) and the vector of main.cpp:220-236
+//     in double.
+//
+// It serves two purposes: it re-decides the windows the FP32 kernel flagged
+// as uncertain, and it is the device FP64 correlation used by the exact
+// per-window API.  One CTA handles one window at a time; CTAs stride over
+// the work list.  FP64 is slow on this part, so the hot path only sends
+// the rare flagged windows here.
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "piv_kernels.h"
+#include "sort_order.h"
+
+namespace opiv {
+
+namespace {
+
+constexpr int kThreads = 64;
+constexpr int kMaxW = 64;
+
+__device__ __forceinline__ double2 e_add(double2 a, double2 b)
+{
+    return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ double2 e_sub(double2 a, double2 b)
+{
+    return make_double2(__dsub_rn(a.x, b.x), __dsub_rn(a.y, b.y));
+}
+// (a + ib)(c + id) = (a*c - b*d, b*c + a*d), pixel_types.h:159-163
+__device__ __forceinline__ double2 e_mul(double2 p, double2 q)
+{
+    return make_double2(__dsub_rn(__dmul_rn(p.x, q.x), __dmul_rn(p.y, q.y)),
+                        __dadd_rn(__dmul_rn(p.y, q.x), __dmul_rn(p.x, q.y)));
+}
+__device__ __forceinline__ double2 e_conj(double2 a) { return make_double2(a.x, -a.y); }
+
+__device__ __forceinline__ double px_d(const uint8_t* p) { return (double)__ldg(p); }
+__device__ __forceinline__ double px_d(const uint16_t* p) { return (double)__ldg(p); }
+__device__ __forceinline__ double px_d(const float* p) { return (double)__ldg(p); }
+__device__ __forceinline__ double px_d(const double* p) { return __ldg(p); }
+
+// In-place radix-2 DIT of n points x[0], x[s], ... (bit-reversal, then
+// butterflies).  tw: table of n entries exp(-+i*pi*j/n).
+__device__ void dit_inplace(double2* x, int n, int s, const double2* tw)
+{
+    int lg = 0;
+    while ((1 << lg) < n) ++lg;
+    for (int i = 0; i < n; ++i) {
+        const int j = (int)(__brev((unsigned)i) >> (32 - lg));
+        if (lg > 0 && i < j) {
+            const double2 t = x[i * s];
+            x[i * s] = x[j * s];
+            x[j * s] = t;
+        }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        const int half = len >> 1, tstep = (2 * n) / len;
+        for (int base = 0; base < n; base += len) {
+            for (int k = 0; k < half; ++k) {
+                const double2 e = x[(base + k) * s];
+                const double2 o = e_mul(x[(base + k + half) * s], tw[k * tstep]);
+                x[(base + k) * s] = e_add(e, o);
+                x[(base + k + half) * s] = e_sub(e, o);
+            }
+        }
+    }
+}
+
+__device__ void fft2d(double2* X, int W, const double2* tw)
+{
+    const int t = threadIdx.x;
+    if (t < W) dit_inplace(X + t * W, W, 1, tw);    // rows
+    __syncthreads();
+    if (t < W) dit_inplace(X + t, W, W, tw);        // columns
+    __syncthreads();
+}
+
+__device__ __forceinline__ void window_origin(const PivParams& p, int64_t w, int& bx, int& by)
+{
+    if (p.win_xy != nullptr) {
+        bx = p.win_xy[2 * w];
+        by = p.win_xy[2 * w + 1];
+    } else {
+        const int64_t gy = w / p.gnx, gx = w - gy * p.gnx;
+        bx = p.gx0 + (int)gx * p.gdx;
+        by = p.gy0 + (int)gy * p.gdy;
+    }
+}
+
+// fit_simple_gaussian's axis function, image_utils.impl.h:86-94
+__device__ __forceinline__ double gauss3(double l, double c, double r)
+{
+    const double num = log(l) - log(r);
+    const double den = 2.0 * (log(l) + log(r) - 2.0 * log(c));
+    if (den == 0.0) return 0.0;
+    return num / den;
+}
+
+template <typename PixT>
+__global__ void __launch_bounds__(kThreads)
+piv_exact_kernel(const PivParams p, int W, int mode, int limit, bool use_list)
+{
+    extern __shared__ double2 sm[];
+    double2* A = sm;               // W*W
+    double2* B = sm + W * W;       // W*W
+    __shared__ int row_count[kMaxW];
+    __shared__ int total_cand;
+
+    const int t = threadIdx.x;
+    const int N = W * W;
+    const int64_t nwork = use_list ? (int64_t)(*p.flag_count) : p.n_win;
+    const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
+    const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
+    const size_t pitch = p.pitch / sizeof(PixT);
+
+    // scan range in plane coordinates (find_peaks on the plane or on its
+    // centre view rect().dilate(0.5); rect.cpp:109-126)
+    int d0 = 0, vw = W;
+    if (limit) {
+        const int rw = (int)lround(0.5 * W);
+        d0 = (W - rw) / 2;
+        vw = rw;
+    }
+    const int sy0 = d0 + 1, sy1 = d0 + vw - 2, sx0 = d0 + 1, sx1 = d0 + vw - 1;
+
+    for (int64_t item = blockIdx.x; item < nwork; item += gridDim.x) {
+        const int64_t w = use_list ? (int64_t)p.flag_list[item] : item;
+        int bx, by;
+        window_origin(p, w, bx, by);
+
+        // ---- extract, convert (g_f by value), join / convert to complex
+        for (int i = t; i < N; i += blockDim.x) {
+            const int y = i / W, x = i % W;
+            const double a = px_d(fa + (size_t)(by + y) * pitch + bx + x);
+            const double b = px_d(fb + (size_t)(by + y) * pitch + bx + x);
+            if (mode == kModeComplex) {
+                A[i] = make_double2(a, 0.0);
+                B[i] = make_double2(b, 0.0);
+            } else {
+                A[i] = make_double2(a, b);
+            }
+        }
+        __syncthreads();
+
+        fft2d(A, W, p.tw_fwd);
+        if (mode == kModeComplex) {
+            fft2d(B, W, p.tw_fwd);
+            for (int i = t; i < N; i += blockDim.x) A[i] = e_mul(B[i], e_conj(A[i]));
+        } else {
+            // transform_real's unpack (fft.h:166-183) fused with the product;
+            // each (k, -k) pair is owned by one thread.  Cells outside the
+            // unpacked set (row 0, row W/2, column 0) become zero.
+            const int npairs = (W / 2 - 1) * (W - 1);
+            for (int q = t; q < npairs; q += blockDim.x) {
+                const int h = 1 + q / (W - 1), x = 1 + q % (W - 1);
+                const int k = h * W + x, m = (W - h) * W + (W - x);
+                const double2 t1 = A[k], t2 = A[m];
+                const double2 half = make_double2(0.5, 0.0);
+                const double2 av = e_mul(half, e_add(t1, e_conj(t2)));
+                double2 bv = e_mul(half, e_sub(t1, e_conj(t2)));
+                bv = make_double2(bv.y, __dmul_rn(-1.0, bv.x));
+                A[k] = e_mul(bv, e_conj(av));
+                A[m] = e_mul(e_conj(bv), e_conj(e_conj(av)));
+            }
+            for (int i = t; i < N; i += blockDim.x) {
+                const int y = i / W, x = i % W;
+                if (y == 0 || y == W / 2 || x == 0) A[i] = make_double2(0.0, 0.0);
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+        fft2d(A, W, p.tw_rev);
+
+        // ---- real part, quadrant swap -> plane in B[].x (row-major)
+        for (int i = t; i < N; i += blockDim.x) {
+            const int y = i / W, x = i % W;
+            const int sy = (y + W / 2) % W, sx = (x + W / 2) % W;
+            B[i].x = A[sy * W + sx].x;
+        }
+        __syncthreads();
+        if (p.planes64 != nullptr)
+            for (int i = t; i < N; i += blockDim.x) p.planes64[(size_t)w * N + i] = B[i].x;
+
+        // ---- find_peaks: strict 4-neighbour maxima of the scanned rows, in
+        // row-major scan order (the order the reference pushes them), then
+        // std::sort's choice of the first one (sort_order.h) and the second
+        // largest value (with multiplicity) for sn.
+        peak_cand* cand = reinterpret_cast<peak_cand*>(A);   // A is free now
+        int my_count = 0;
+        const int y = t;
+        const bool row_ok = t < W && y >= sy0 && y < sy1;
+        if (row_ok) {
+            for (int x = sx0; x < sx1; ++x) {
+                const double c = B[y * W + x].x;
+                if (B[y * W + x - 1].x < c && B[y * W + x + 1].x < c &&
+                    B[(y - 1) * W + x].x < c && B[(y + 1) * W + x].x < c)
+                    ++my_count;
+            }
+        }
+        if (t < W) row_count[t] = my_count;
+        __syncthreads();
+        if (t == 0) {
+            int acc = 0;
+            for (int r = 0; r < W; ++r) {
+                const int c = row_count[r];
+                row_count[r] = acc;
+                acc += c;
+            }
+            total_cand = acc;
+        }
+        __syncthreads();
+        if (row_ok) {
+            int o = row_count[t];
+            for (int x = sx0; x < sx1; ++x) {
+                const double c = B[y * W + x].x;
+                if (B[y * W + x - 1].x < c && B[y * W + x + 1].x < c &&
+                    B[(y - 1) * W + x].x < c && B[(y + 1) * W + x].x < c)
+                    cand[o++] = peak_cand{ c, y * W + x };
+            }
+        }
+        __syncthreads();
+        if (t == 0) {
+            const int n = total_cand;
+            const double ninf = -__longlong_as_double(0x7ff0000000000000ll);
+            double g0 = ninf, g1 = ninf;   // two largest values, with multiplicity
+            for (int i = 0; i < n; ++i) {
+                const double c = cand[i].v;
+                if (c > g0) { g1 = g0; g0 = c; }
+                else if (c > g1) g1 = c;
+            }
+            int k = -1;
+            if (n >= 2) {
+                sort_order_head(cand, n);
+                k = cand[0].key;
+            }
+            const int count = n >= 2 ? 2 : n;
+            opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
+            int32_t code = -1;
+            if (count == 2) {
+                const int px = k % W, py = k / W;
+                const double c = B[py * W + px].x;
+                const double lx = (double)px + gauss3(B[py * W + px - 1].x, c, B[py * W + px + 1].x);
+                const double ly = (double)py + gauss3(B[(py - 1) * W + px].x, c, B[(py + 1) * W + px].x);
+                const int mx = bx + W / 2, my = by + W / 2;
+                out.x = (float)mx;
+                out.y = (float)((double)p.img_h - (double)my);
+                out.u = (float)((double)mx - ((double)bx + lx));
+                out.v = (float)((double)my - ((double)by + ly));
+                out.sn = (g1 > 0) ? (float)(g0 / g1) : 0.f;
+                code = k | OPIV_PEAK_EXACT;
+            }
+            if (p.out_vec) p.out_vec[w] = out;
+            if (p.out_peak) p.out_peak[w] = code;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename PixT>
+cudaError_t launch_t(const PivParams& p, int w, int mode, int limit, bool use_list, int blocks,
+                     cudaStream_t s)
+{
+    const size_t smem = 2 * sizeof(double2) * (size_t)w * w;
+    cudaError_t e = cudaFuncSetAttribute(piv_exact_kernel<PixT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    piv_exact_kernel<PixT><<<blocks, kThreads, smem, s>>>(p, w, mode, limit, use_list);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool exact_supports(int w) { return w >= 4 && w <= kMaxW && (w & (w - 1)) == 0; }
+
+cudaError_t launch_piv_exact(const PivParams& p, int w, int dtype, int mode, int limit,
+                             bool use_list, int blocks, cudaStream_t s)
+{
+    if (!exact_supports(w) || blocks <= 0) return cudaErrorInvalidValue;
+    switch (dtype) {
+    case kU8: return launch_t<uint8_t>(p, w, mode, limit, use_list, blocks, s);
+    case kU16: return launch_t<uint16_t>(p, w, mode, limit, use_list, blocks, s);
+    case kF32: return launch_t<float>(p, w, mode, limit, use_list, blocks, s);
+    case kF64: return launch_t<double>(p, w, mode, limit, use_list, blocks, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace opiv

@@ -1,0 +1,60 @@
+// piv_kernels.h -- launch interface between the C ABI layer and the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "openpiv_gb300.h"
+
+namespace opiv {
+
+enum { kModeReal = OPIV_CORR_REAL, kModeComplex = OPIV_CORR_COMPLEX };
+enum { kU8 = OPIV_U8, kU16 = OPIV_U16, kF32 = OPIV_F32, kF64 = 3 /* internal: batch API */ };
+
+// Everything one pass over an image pair needs on the device.
+struct PivParams {
+    const void* fa = nullptr;          // frame A (device), img_h rows of `pitch` bytes
+    const void* fb = nullptr;          // frame B
+    size_t pitch = 0;                  // bytes per row
+    int img_w = 0, img_h = 0;
+    // regular grid: window k at (gx0 + (k % gnx) * gdx, gy0 + (k / gnx) * gdy)
+    int gx0 = 0, gy0 = 0, gdx = 0, gdy = 0, gnx = 1;
+    const int32_t* win_xy = nullptr;   // explicit (x, y) list overrides the grid
+    int64_t n_win = 0;
+    opiv_vector* out_vec = nullptr;
+    int32_t* out_peak = nullptr;       // may be null
+    // windows whose FP32 decisions are not certain (see piv_fp32.cu)
+    unsigned int* flag_count = nullptr;
+    int32_t* flag_list = nullptr;
+    float kappa = 16.f;                // FP32 error-bound factor
+    // debug / per-window API outputs
+    float* planes = nullptr;           // FP32 kernel: n_win * W * W (mean-free part)
+    double* peds = nullptr;            // FP32 kernel: per-window pedestal
+    double* planes64 = nullptr;        // exact kernel: n_win * W * W full planes
+    // exact pass
+    const double2* tw_fwd = nullptr;   // reference twiddle tables for length W
+    const double2* tw_rev = nullptr;
+};
+
+// Fused FP32 kernel, one entry per window size (piv_fp32_w*.cu).  Frames
+// (u8/u16/f32) without plane output; double windows (kF64) with planes.
+cudaError_t launch_piv_fp32_w16(const PivParams& p, int dtype, int mode, int limit, bool planes,
+                                cudaStream_t s);
+cudaError_t launch_piv_fp32_w32(const PivParams& p, int dtype, int mode, int limit, bool planes,
+                                cudaStream_t s);
+inline bool fp32_supports(int w) { return w == 16 || w == 32; }
+inline cudaError_t launch_piv_fp32(const PivParams& p, int w, int dtype, int mode, int limit,
+                                   bool planes, cudaStream_t s)
+{
+    if (w == 16) return launch_piv_fp32_w16(p, dtype, mode, limit, planes, s);
+    if (w == 32) return launch_piv_fp32_w32(p, dtype, mode, limit, planes, s);
+    return cudaErrorInvalidValue;
+}
+
+// Exact double-precision re-evaluation.  When `list_count` is non-null the
+// kernel processes the windows listed in flag_list[0 .. *list_count);
+// otherwise all n_win windows.  `blocks` CTAs stride over the work.
+bool exact_supports(int w);
+cudaError_t launch_piv_exact(const PivParams& p, int w, int dtype, int mode, int limit,
+                             bool use_list, int blocks, cudaStream_t s);
+
+}  // namespace opiv

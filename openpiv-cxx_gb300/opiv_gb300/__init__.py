@@ -1,0 +1,253 @@
+"""Python binding of the GB300 PIV path -- a thin ctypes layer over the C ABI
+declared in include/openpiv_gb300.h (libopenpiv_gb300.so, built in-tree by
+openpiv-cxx_gb300/build.py).
+
+There is no fallback: if the shared library is missing, importing the
+functions below raises.  Errors of the C ABI become ``OpivError`` carrying
+the status code and the library's message (which starts with the text of
+the exception the reference throws for the same condition).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libopenpiv_gb300.so")
+
+U8, U16, F32 = 0, 1, 2
+CORR_REAL, CORR_COMPLEX = 0, 1
+PEAK_EXACT = 0x40000000
+PEAK_MASK = 0x0000FFFF
+
+OK = 0
+ERR_OFFSET_RANGE = -1
+ERR_IMAGE_EMPTY = -2
+ERR_IA_EMPTY = -3
+ERR_OFFSET_ZERO = -4
+ERR_IA_TOO_BIG = -5
+ERR_NOT_POW2 = -6
+ERR_CAPACITY = -7
+ERR_RECT_OUTSIDE = -8
+ERR_ARG = -9
+ERR_SIZE_MISMATCH = -10
+ERR_UNSUPPORTED = -11
+ERR_CUDA = -12
+ERR_NO_DEVICE = -13
+
+DTYPES = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
+SYMBOLS = [
+    "opiv_last_error", "opiv_status_string", "opiv_version", "opiv_kernel_launch_count",
+    "opiv_grid", "opiv_grid_offsets", "opiv_plan_create", "opiv_plan_destroy",
+    "opiv_plan_window_count", "opiv_plan_grid", "opiv_process_pair",
+    "opiv_process_pair_device", "opiv_plan_exact_count", "opiv_plan_set_timing",
+    "opiv_plan_last_timing", "opiv_cross_correlate_batch",
+    "opiv_find_peaks", "opiv_fit_simple_gaussian",
+]
+
+VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
+                         ("v", np.float32), ("sn", np.float32)])
+
+
+class OpivError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+        self.message = message
+
+
+_lib = None
+_ip = C.POINTER(C.c_int32)
+_dp = C.POINTER(C.c_double)
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Loads the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run build() (the GPU path has no fallback)")
+    L = C.CDLL(path)
+    L.opiv_last_error.restype = C.c_char_p
+    L.opiv_status_string.restype = C.c_char_p
+    L.opiv_status_string.argtypes = [C.c_int]
+    L.opiv_kernel_launch_count.restype = C.c_int64
+    L.opiv_grid.restype = C.c_int64
+    L.opiv_grid.argtypes = [C.c_uint32] * 4 + [C.c_double, _ip, C.c_int64]
+    L.opiv_grid_offsets.restype = C.c_int64
+    L.opiv_grid_offsets.argtypes = [C.c_uint32] * 6 + [_ip, C.c_int64]
+    L.opiv_plan_create.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_int,
+                                   C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_int]
+    L.opiv_plan_destroy.argtypes = [C.c_void_p]
+    L.opiv_plan_window_count.restype = C.c_int64
+    L.opiv_plan_window_count.argtypes = [C.c_void_p]
+    L.opiv_plan_grid.argtypes = [C.c_void_p, _ip, C.c_int64]
+    L.opiv_process_pair.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+                                    C.c_void_p]
+    L.opiv_process_pair_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                           C.c_void_p, C.c_void_p, C.c_void_p]
+    L.opiv_plan_exact_count.restype = C.c_int64
+    L.opiv_plan_exact_count.argtypes = [C.c_void_p]
+    L.opiv_plan_set_timing.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.opiv_cross_correlate_batch.argtypes = [_dp, _dp, C.c_uint32, C.c_int64, C.c_int, C.c_int,
+                                             _dp, C.c_int]
+    L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
+    L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
+    _lib = L
+    return L
+
+
+def _check(status: int) -> int:
+    if status < 0:
+        raise OpivError(int(status), load().opiv_last_error().decode())
+    return status
+
+
+def last_error() -> str:
+    return load().opiv_last_error().decode()
+
+
+def kernel_launch_count() -> int:
+    return int(load().opiv_kernel_launch_count())
+
+
+# ---- grid ------------------------------------------------------------------
+def grid(img_w: int, img_h: int, ia_w: int, ia_h: int, step_fraction: float) -> np.ndarray:
+    """core::generate_cartesian_grid(size, size, double): (n, 2) int32 corners."""
+    L = load()
+    n = _check(L.opiv_grid(img_w, img_h, ia_w, ia_h, step_fraction, None, 0))
+    out = np.zeros((n, 2), np.int32)
+    _check(L.opiv_grid(img_w, img_h, ia_w, ia_h, step_fraction, out.ctypes.data_as(_ip), n))
+    return out
+
+
+def grid_offsets(img_w: int, img_h: int, ia_w: int, ia_h: int, dx: int, dy: int) -> np.ndarray:
+    L = load()
+    n = _check(L.opiv_grid_offsets(img_w, img_h, ia_w, ia_h, dx, dy, None, 0))
+    out = np.zeros((n, 2), np.int32)
+    _check(L.opiv_grid_offsets(img_w, img_h, ia_w, ia_h, dx, dy, out.ctypes.data_as(_ip), n))
+    return out
+
+
+# ---- plans -----------------------------------------------------------------
+class Plan:
+    """One image geometry + window size + grid step + correlation mode."""
+
+    def __init__(self, img_w: int, img_h: int, dtype, ia: int, dx: int, dy: int | None = None,
+                 mode: int = CORR_COMPLEX, limit_search: bool = False, device: int = 0):
+        L = load()
+        dy = dx if dy is None else dy
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in DTYPES:
+            raise OpivError(ERR_ARG, f"unsupported pixel type {self.dtype}")
+        h = C.c_void_p()
+        _check(L.opiv_plan_create(C.byref(h), img_w, img_h, DTYPES[self.dtype], ia, dx, dy, mode,
+                                  int(bool(limit_search)), device))
+        self._h = h
+        self.img_w, self.img_h, self.ia, self.dx, self.dy = img_w, img_h, ia, dx, dy
+        self.mode, self.limit_search = mode, bool(limit_search)
+        self.n = int(L.opiv_plan_window_count(h))
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().opiv_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def grid(self) -> np.ndarray:
+        out = np.zeros((self.n, 2), np.int32)
+        _check(load().opiv_plan_grid(self._h, out.ctypes.data_as(_ip), self.n))
+        return out
+
+    def process(self, frame_a: np.ndarray, frame_b: np.ndarray, with_peaks: bool = True):
+        """Host arrays in, (vectors (n, 5) float32, peak codes (n,) int32) out."""
+        for f in (frame_a, frame_b):
+            if f.dtype != self.dtype or f.shape != (self.img_h, self.img_w):
+                raise OpivError(ERR_SIZE_MISMATCH,
+                                f"image size is different from expected: {f.shape} {f.dtype}")
+        fa = np.ascontiguousarray(frame_a)
+        fb = np.ascontiguousarray(frame_b)
+        vec = np.zeros((self.n, 5), np.float32)
+        pk = np.zeros(self.n, np.int32) if with_peaks else None
+        _check(load().opiv_process_pair(self._h, fa.ctypes.data, fb.ctypes.data, fa.strides[0],
+                                        vec.ctypes.data, pk.ctypes.data if with_peaks else None))
+        return vec, pk
+
+    def process_into(self, pa: int, pb: int, pitch: int, out_vec: int, out_peak: int | None):
+        """Host pointers (e.g. pinned buffers) in and out; synchronous."""
+        _check(load().opiv_process_pair(self._h, pa, pb, pitch, out_vec, out_peak))
+
+    def process_device(self, d_a: int, d_b: int, pitch: int, d_vec: int, d_peak: int | None,
+                       stream: int = 0):
+        """Device pointers; asynchronous on `stream` (a cudaStream_t value)."""
+        _check(load().opiv_process_pair_device(self._h, d_a, d_b, pitch, d_vec, d_peak,
+                                               stream or None))
+
+    def exact_count(self) -> int:
+        return int(load().opiv_plan_exact_count(self._h))
+
+    def set_timing(self, enable: bool = True):
+        _check(load().opiv_plan_set_timing(self._h, int(bool(enable))))
+
+    def last_timing(self) -> tuple[float, float]:
+        """(FP32 kernel ms, exact pass ms) of the last pass."""
+        a, b = C.c_float(), C.c_float()
+        _check(load().opiv_plan_last_timing(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+
+# ---- per-window API --------------------------------------------------------
+def cross_correlate_batch(a: np.ndarray, b: np.ndarray, mode: int, exact: bool = False,
+                          device: int = 0) -> np.ndarray:
+    """FFT::cross_correlate[_real] on (n, w, w) window stacks -> (n, w, w) planes."""
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    if a.ndim == 2:
+        a, b = a[None], b[None]
+    if a.shape != b.shape:
+        raise OpivError(ERR_SIZE_MISMATCH, f"image size is different from expected: {a.shape}")
+    n, h, w = a.shape
+    if h != w:
+        raise OpivError(ERR_UNSUPPORTED, f"no kernel for {w}x{h} windows")
+    out = np.zeros((n, w, w), np.float64)
+    _check(load().opiv_cross_correlate_batch(a.ctypes.data_as(_dp), b.ctypes.data_as(_dp), w, n,
+                                             mode, int(bool(exact)), out.ctypes.data_as(_dp),
+                                             device))
+    return out
+
+
+def find_peaks(im: np.ndarray, num_peaks: int, radius: int = 1):
+    im = np.ascontiguousarray(im, np.float64)
+    h, w = im.shape
+    xy = np.zeros((max(num_peaks, 1), 2), np.int32)
+    v = np.zeros(max(num_peaks, 1), np.float64)
+    n = _check(load().opiv_find_peaks(im.ctypes.data_as(_dp), w, h, num_peaks, radius,
+                                      xy.ctypes.data_as(_ip), v.ctypes.data_as(_dp)))
+    return xy[:n], v[:n]
+
+
+def fit_simple_gaussian(plane: np.ndarray, px: int, py: int) -> np.ndarray:
+    plane = np.ascontiguousarray(plane, np.float64)
+    out = np.zeros(2, np.float64)
+    _check(load().opiv_fit_simple_gaussian(plane.ctypes.data_as(_dp), plane.shape[1],
+                                           plane.shape[0], px, py, out.ctypes.data_as(_dp)))
+    return out

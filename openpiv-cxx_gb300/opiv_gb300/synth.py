@@ -1,0 +1,101 @@
+"""Seeded synthetic PIV image pairs (particle images).
+
+The reference names no public dataset; its workloads are described by
+particle statistics, so inputs are generated here:
+  * particles at `ppp` per pixel, positions uniform in [-4, W+4) x [-4, H+4)
+    (no depletion at the edges);
+  * each particle is a Gaussian spot I0 * exp(-8 r^2 / d^2), r measured from
+    the pixel centre (x + 0.5, y + 0.5), d ~ N(2.5, 0.5) clipped to [1.5, 4];
+  * frame B holds the same particles moved by the displacement field
+    evaluated at each particle;
+  * N(0, sigma) noise is added, then values are rounded half-to-even and
+    clipped to the signal range of the pixel type (float frames are not
+    rounded).
+RNG: numpy PCG64, seed = 20261203 + 1000 * config + pair index.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+SEED_BASE = 20261203
+STAMP = 6   # stamp half-width in pixels (exp(-8 r^2/d^2) * 4000 < 1e-5 beyond it)
+
+
+def _render(h: int, w: int, px: np.ndarray, py: np.ndarray, d: np.ndarray, i0: np.ndarray,
+            chunk: int = 1 << 16) -> np.ndarray:
+    img = np.zeros(h * w, np.float64)
+    offs = np.arange(-STAMP, STAMP + 1)
+    for s in range(0, px.size, chunk):
+        cx, cy = px[s:s + chunk], py[s:s + chunk]
+        dd, ii = d[s:s + chunk], i0[s:s + chunk]
+        ix = np.floor(cx).astype(np.int64)[:, None] + offs[None, :]     # (n, k)
+        iy = np.floor(cy).astype(np.int64)[:, None] + offs[None, :]
+        gx = np.exp(-8.0 * ((ix + 0.5) - cx[:, None]) ** 2 / (dd[:, None] ** 2))
+        gy = np.exp(-8.0 * ((iy + 0.5) - cy[:, None]) ** 2 / (dd[:, None] ** 2))
+        val = ii[:, None, None] * gy[:, :, None] * gx[:, None, :]       # (n, ky, kx)
+        yy = np.broadcast_to(iy[:, :, None], val.shape)
+        xx = np.broadcast_to(ix[:, None, :], val.shape)
+        m = (xx >= 0) & (xx < w) & (yy >= 0) & (yy < h)
+        img += np.bincount((yy[m] * w + xx[m]).ravel(), weights=val[m].ravel(), minlength=h * w)
+    return img.reshape(h, w)
+
+
+def particle_pair(h: int, w: int, *, ppp: float, i0_range: tuple[float, float], noise: float,
+                  displacement, dtype, seed: int, full_scale: float | None = None,
+                  d_mean: float = 2.5, d_std: float = 0.5):
+    """Returns (frame_a, frame_b) of shape (h, w) and pixel type `dtype`.
+
+    displacement(x, y) -> (u, v) in pixels, x to the right, y down (rows).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = int(round(ppp * w * h))
+    x = rng.uniform(-4.0, w + 4.0, n)
+    y = rng.uniform(-4.0, h + 4.0, n)
+    d = np.clip(rng.normal(d_mean, d_std, n), 1.5, 4.0)
+    i0 = rng.uniform(i0_range[0], i0_range[1], n)
+    u, v = displacement(x, y)
+    a = _render(h, w, x, y, d, i0)
+    b = _render(h, w, x + u, y + v, d, i0)
+    a += rng.normal(0.0, noise, a.shape)
+    b += rng.normal(0.0, noise, b.shape)
+    dt = np.dtype(dtype)
+    if dt.kind == "u":
+        hi = full_scale if full_scale is not None else float(np.iinfo(dt).max)
+        a = np.clip(np.rint(a), 0, hi).astype(dt)
+        b = np.clip(np.rint(b), 0, hi).astype(dt)
+    else:
+        lo, hi = (0.0, full_scale) if full_scale is not None else (-np.inf, np.inf)
+        a = np.clip(a, lo, hi).astype(dt)
+        b = np.clip(b, lo, hi).astype(dt)
+    return a, b
+
+
+# ---- the workloads -----------------------------------------------------------
+def config1(pair: int = 0):
+    """1024^2 uint8, ppp 0.02, I0 ~ U(150, 255), sigma 3, uniform (2.35, -1.70) px.
+    Windows 32 x 32 at step fraction 0.5 (3969 windows)."""
+    return particle_pair(1024, 1024, ppp=0.02, i0_range=(150, 255), noise=3.0,
+                         displacement=lambda x, y: (np.full_like(x, 2.35), np.full_like(y, -1.70)),
+                         dtype=np.uint8, seed=SEED_BASE + 1000 * 1 + pair)
+
+
+def config2_field(x, y):
+    return 3.0 * np.sin(2 * math.pi * y / 1024.0), 2.0 * np.cos(2 * math.pi * x / 768.0)
+
+
+def config2(pair: int = 0, size: int = 4096):
+    """4096^2 uint16 (12-bit signal), ppp 0.03, I0 ~ U(1500, 4000), sigma 20,
+    u = 3 sin(2 pi y / 1024), v = 2 cos(2 pi x / 768).  Windows 32 x 32 at
+    step 8 (509 x 509 = 259,081 windows)."""
+    return particle_pair(size, size, ppp=0.03, i0_range=(1500, 4000), noise=20.0,
+                         displacement=config2_field, dtype=np.uint16,
+                         seed=SEED_BASE + 1000 * 2 + pair, full_scale=4095.0)
+
+
+def config5(pair: int = 0, size: int = 2048):
+    """2048^2 float32 in [0, 1], ppp 0.02, I0 ~ U(0.6, 1), sigma 0.02, shift (0.40, 0.25)."""
+    return particle_pair(size, size, ppp=0.02, i0_range=(0.6, 1.0), noise=0.02,
+                         displacement=lambda x, y: (np.full_like(x, 0.40), np.full_like(y, 0.25)),
+                         dtype=np.float32, seed=SEED_BASE + 1000 * 5 + pair, full_scale=1.0)

@@ -1,0 +1,99 @@
+"""C ABI checks that need no GPU: the library loads, exports every symbol the
+header declares, and its host-side parts (grids, argument validation, the
+host find_peaks / fit_simple_gaussian) agree with the oracle."""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import opiv_gb300 as og
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "openpiv_gb300.h")
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(opiv_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_symbols()
+    assert len(names) >= 16
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in the header but not exported"
+    assert set(names) == set(og.SYMBOLS)
+
+
+def test_status_strings(lib):
+    assert og.load().opiv_status_string(og.ERR_NOT_POW2).decode() == "dimensions must be power of 2"
+    assert og.load().opiv_status_string(og.ERR_OFFSET_ZERO).decode() == "offsets must be non-zero"
+
+
+@pytest.mark.parametrize("case", json.load(open(os.path.join(GOLDEN, "reference_kats.json")))["grid"],
+                         ids=lambda c: c["cite"])
+def test_grid_kats(lib, case):
+    (iw, ih), (aw, ah) = case["image"], case["ia"]
+    if "frac" in case:
+        g = og.grid(iw, ih, aw, ah, case["frac"])
+    else:
+        g = og.grid_offsets(iw, ih, aw, ah, *case["offsets"])
+    assert sorted(map(tuple, g.tolist())) == sorted(map(tuple, case["origins"]))
+
+
+@pytest.mark.parametrize("args", [(1024, 1024, 32, 32, 0.5), (4096, 4096, 32, 32, 0.25),
+                                  (1000, 700, 16, 16, 0.5), (517, 333, 64, 64, 0.75),
+                                  (2048, 1536, 64, 64, 0.5), (33, 32, 32, 32, 1.0)])
+def test_grid_matches_oracle(lib, orc, args):
+    assert np.array_equal(og.grid(*args), orc.grid(*args))
+
+
+@pytest.mark.parametrize("args,status,msg", [
+    ((100, 100, 32, 32, 1.5), og.ERR_OFFSET_RANGE, "offsets must be between 0.0 and 1.0"),
+    ((0, 100, 32, 32, 0.5), og.ERR_IMAGE_EMPTY, "image size must be non-zero"),
+    ((100, 100, 0, 32, 0.5), og.ERR_IA_EMPTY, "interrogation size must be non-zero"),
+    ((100, 100, 32, 32, 0.01), og.ERR_OFFSET_ZERO, "offsets must be non-zero"),
+    ((16, 100, 32, 32, 0.5), og.ERR_IA_TOO_BIG, "interrogation size is bigger than image"),
+])
+def test_grid_errors(lib, args, status, msg):
+    with pytest.raises(og.OpivError) as e:
+        og.grid(*args)
+    assert e.value.status == status
+    assert e.value.message.startswith(msg)
+
+
+def test_plan_validation_precedes_device(lib):
+    """Argument errors are reported before any device is touched, in the
+    reference's order (grid checks, then the FFT's power-of-two check)."""
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(100, 100, np.uint8, 24, 8)
+    assert e.value.status == og.ERR_NOT_POW2
+    assert "power of 2" in e.value.message
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(100, 100, np.uint8, 128, 8)
+    assert e.value.status == og.ERR_IA_TOO_BIG
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(100, 100, np.uint8, 32, 0)
+    assert e.value.status == og.ERR_OFFSET_ZERO
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(100, 100, np.int32, 32, 8)
+    assert e.value.status == og.ERR_ARG
+
+
+def test_host_find_peaks_and_fit(lib, orc):
+    rng = np.random.default_rng(1)
+    for _ in range(20):
+        im = rng.normal(size=(32, 32))
+        xy1, v1 = og.find_peaks(im, 5, 1)
+        xy2, v2 = orc.find_peaks(im, 5, 1)
+        assert np.array_equal(xy1, xy2) and np.array_equal(v1, v2)
+        plane = np.abs(im) + 1.0
+        px, py = int(rng.integers(1, 31)), int(rng.integers(1, 31))
+        assert np.array_equal(og.fit_simple_gaussian(plane, px, py),
+                              orc.fit_simple_gaussian(plane, px, py))
+    with pytest.raises(og.OpivError):
+        og.fit_simple_gaussian(np.ones((32, 32)), 0, 5)

@@ -1,0 +1,254 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the oracle
+(CPU restatement of the reference, itself pinned to the compiled reference)
+and against committed outputs of the compiled reference.
+
+Tolerances (from the path's specification):
+  * grid coordinates and integer peak locations: bit-exact;
+  * FP32 correlation planes: within 1e-5 of the plane's peak magnitude;
+  * exact-mode planes: bit-identical;
+  * sub-pixel displacements u, v: within 1e-4 px; NaN where the reference
+    has NaN (its log of a non-positive neighbour);
+  * x, y: exact; sn: within 1e-5 relative (0 where the reference has 0).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import opiv_gb300 as og
+from opiv_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+UV_TOL = 1e-4
+SN_RTOL = 1e-5
+PLANE_RTOL = 1e-5
+THREADS = os.cpu_count() or 4
+
+
+def peak_codes(ref_pk, w):
+    return np.where(ref_pk[:, 0] >= 0, ref_pk[:, 1] * w + ref_pk[:, 0], -1)
+
+
+def gpu_codes(pk):
+    return np.where(pk >= 0, pk & og.PEAK_MASK, -1)
+
+
+def assert_vectors_match(vec, pk, ref_vec, ref_pk, w, what=""):
+    ref_code = peak_codes(ref_pk, w)
+    got_code = gpu_codes(pk)
+    bad = np.nonzero(got_code != ref_code)[0]
+    assert bad.size == 0, f"{what}: {bad.size} integer peaks differ, first windows {bad[:8]}"
+    v = vec.astype(np.float64)
+    assert np.array_equal(v[:, 0:2], ref_vec[:, 0:2]), f"{what}: x, y differ"
+    nan_ref = np.isnan(ref_vec[:, 2:4])
+    assert np.array_equal(np.isnan(v[:, 2:4]), nan_ref), f"{what}: NaN pattern differs"
+    d = np.where(nan_ref, 0.0, np.abs(v[:, 2:4] - ref_vec[:, 2:4]))
+    assert d.max(initial=0.0) <= UV_TOL, f"{what}: max |du|,|dv| = {d.max()}"
+    sn_ref = ref_vec[:, 4]
+    assert np.array_equal(v[:, 4] == 0, sn_ref == 0), f"{what}: sn zero pattern differs"
+    rel = np.abs(v[:, 4] - sn_ref) / np.maximum(np.abs(sn_ref), 1e-30)
+    rel = np.where(sn_ref == 0, 0.0, rel)
+    assert rel.max(initial=0.0) <= SN_RTOL, f"{what}: max sn relative error {rel.max()}"
+
+
+def run_both(orc, a, b, ia, step, mode, limit, dtype=None):
+    h, w = a.shape
+    plan = og.Plan(w, h, a.dtype if dtype is None else dtype, ia, step, mode=mode,
+                   limit_search=limit)
+    vec, pk = plan.process(a, b)
+    grid = plan.grid()
+    ref_vec, ref_pk, _ = orc.process_windows(a.astype(np.float64), b.astype(np.float64), grid, ia,
+                                             mode, limit, THREADS)
+    exact = plan.exact_count()
+    plan.close()
+    return vec, pk, ref_vec, ref_pk, exact
+
+
+# ---- correlation planes ----------------------------------------------------
+@pytest.mark.parametrize("w", [8, 16, 32, 64])
+@pytest.mark.parametrize("mode", [og.CORR_REAL, og.CORR_COMPLEX])
+def test_exact_planes_bit_identical(orc, w, mode):
+    rng = np.random.default_rng(100 + w + mode)
+    a = rng.integers(0, 4096, (6, w, w)).astype(np.float64)
+    b = rng.integers(0, 4096, (6, w, w)).astype(np.float64)
+    got = og.cross_correlate_batch(a, b, mode, exact=True)
+    for k in range(a.shape[0]):
+        ref = orc.cross_correlate(a[k], b[k], mode)
+        assert np.array_equal(got[k], ref), f"window {k}: max diff {np.abs(got[k] - ref).max()}"
+
+
+@pytest.mark.parametrize("w", [16, 32])
+@pytest.mark.parametrize("mode", [og.CORR_REAL, og.CORR_COMPLEX])
+def test_fp32_planes_within_tolerance(orc, w, mode):
+    rng = np.random.default_rng(200 + w + mode)
+    a = rng.integers(0, 4096, (16, w, w)).astype(np.float64)
+    b = np.roll(a, (1, 2), (1, 2)) + rng.integers(0, 200, a.shape)
+    got = og.cross_correlate_batch(a, b, mode, exact=False)
+    for k in range(a.shape[0]):
+        ref = orc.cross_correlate(a[k], b[k], mode)
+        err = np.abs(got[k] - ref).max()
+        assert err <= PLANE_RTOL * np.abs(ref).max(), f"window {k}: {err}"
+        if mode == og.CORR_COMPLEX:   # the mean-free part alone, same bound
+            ped = a[k].sum() * b[k].sum()
+            assert err <= PLANE_RTOL * np.abs(ref - ped).max()
+
+
+def test_planes_vs_reference_fixture():
+    z = np.load(os.path.join(GOLDEN, "ref_outputs.npz"))
+    for name in ("u8_w32", "u16_w32", "u16_w16"):
+        a, b, grid = z[f"{name}/a"], z[f"{name}/b"], z[f"{name}/grid"]
+        ia = int(z[f"{name}/meta"][0])
+        sel = z[f"{name}/planes_sel"]
+        wa = np.stack([a[y:y + ia, x:x + ia] for x, y in grid[sel]]).astype(np.float64)
+        wb = np.stack([b[y:y + ia, x:x + ia] for x, y in grid[sel]]).astype(np.float64)
+        for mode, mname in ((0, "real"), (1, "complex")):
+            ref = z[f"{name}/planes_{mname}"]
+            assert np.array_equal(og.cross_correlate_batch(wa, wb, mode, exact=True), ref)
+            got = og.cross_correlate_batch(wa, wb, mode, exact=False)
+            for k in range(len(sel)):
+                assert np.abs(got[k] - ref[k]).max() <= PLANE_RTOL * np.abs(ref[k]).max()
+
+
+# ---- whole passes ---------------------------------------------------------
+def test_process_vs_reference_fixtures():
+    z = np.load(os.path.join(GOLDEN, "ref_outputs.npz"))
+    for name in ("u8_w32", "u16_w32", "u16_w16"):
+        a, b, grid = z[f"{name}/a"], z[f"{name}/b"], z[f"{name}/grid"]
+        ia, step = (int(v) for v in z[f"{name}/meta"])
+        h, w = a.shape
+        for mode, mname in ((0, "real"), (1, "complex")):
+            for limit in (0, 1):
+                plan = og.Plan(w, h, a.dtype, ia, step, mode=mode, limit_search=limit)
+                assert np.array_equal(plan.grid(), grid)
+                vec, pk = plan.process(a, b)
+                assert_vectors_match(vec, pk, z[f"{name}/vec_{mname}_{limit}"],
+                                     z[f"{name}/peak_{mname}_{limit}"], ia, f"{name} {mname} {limit}")
+                plan.close()
+
+
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+@pytest.mark.parametrize("limit", [False, True])
+def test_config1_uint8_1024(orc, mode, limit):
+    a, b = synth.config1()
+    vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 32, 16, mode, limit)
+    assert vec.shape[0] == 3969
+    assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, "config1")
+    if mode == og.CORR_COMPLEX and not limit:
+        u = vec[:, 2].astype(np.float64)
+        good = np.abs(u + 2.35) < 0.5
+        assert good.mean() > 0.9   # the reference convention: u = -shift
+
+
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_config2_uint16_4096_full(orc, mode):
+    """All 259,081 windows of the 4096^2 12-bit pair at step 8."""
+    a, b = synth.config2()
+    vec, pk, ref_vec, ref_pk, exact = run_both(orc, a, b, 32, 8, mode, False)
+    assert vec.shape[0] == 509 * 509
+    assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, f"config2 mode {mode}")
+    print(f"config2 mode {mode}: {exact} windows re-decided by the exact pass")
+
+
+def test_w16_uint16(orc):
+    a, b = synth.config2(size=1024)
+    for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+        for limit in (False, True):
+            vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 16, 4, mode, limit)
+            assert_vectors_match(vec, pk, ref_vec, ref_pk, 16, f"w16 {mode} {limit}")
+
+
+def test_float32_frames(orc):
+    a, b = synth.config5(size=512)
+    for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+        vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 32, 16, mode, False)
+        assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, f"f32 {mode}")
+
+
+# ---- edge cases ------------------------------------------------------------
+@pytest.mark.parametrize("value", [0, 1, 4095, 65535])
+def test_constant_frames_give_no_peaks(orc, value):
+    a = np.full((96, 128), value, np.uint16)
+    for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+        vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, a.copy(), 32, 16, mode, False)
+        assert np.all(pk == -1) and np.all(vec == 0)
+        assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, "constant")
+
+
+def test_single_window_and_margins(orc):
+    rng = np.random.default_rng(9)
+    for (h, w), step in (((32, 32), 16), ((70, 100), 16), ((33, 65), 8), ((47, 131), 13)):
+        a = rng.integers(0, 256, (h, w)).astype(np.uint8)
+        b = np.roll(a, (1, -2), (0, 1))
+        for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+            vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 32, step, mode, False)
+            assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, f"{h}x{w}/{step}")
+
+
+def test_saturated_uint16_full_range(orc):
+    rng = np.random.default_rng(4)
+    a = rng.integers(60000, 65536, (128, 128)).astype(np.uint16)
+    b = np.roll(a, (3, 1), (0, 1))
+    for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+        vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 32, 8, mode, False)
+        assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, "saturated")
+
+
+def test_periodic_windows_use_exact_pass(orc):
+    """Periodic windows give exactly tied correlation peaks; the FP32 pass
+    must hand them to the exact pass, which must pick the same peak as the
+    reference's std::sort."""
+    rng = np.random.default_rng(21)
+    tile = rng.integers(0, 256, (8, 8)).astype(np.uint8)
+    a = np.tile(tile, (16, 16))
+    b = np.roll(a, (2, 3), (0, 1))
+    for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+        vec, pk, ref_vec, ref_pk, exact = run_both(orc, a, b, 32, 16, mode, False)
+        assert exact > 0
+        assert np.any(pk & og.PEAK_EXACT)
+        assert_vectors_match(vec, pk, ref_vec, ref_pk, 32, f"periodic {mode}")
+
+
+# ---- API behaviour ---------------------------------------------------------
+def test_two_launches_per_pass():
+    a, b = synth.config1()
+    plan = og.Plan(1024, 1024, np.uint8, 32, 16)
+    n0 = og.kernel_launch_count()
+    plan.process(a, b)
+    assert og.kernel_launch_count() - n0 == 2
+
+
+def test_device_buffers_match_host_call():
+    torch = pytest.importorskip("torch")
+    a, b = synth.config1()
+    plan = og.Plan(1024, 1024, np.uint8, 32, 16)
+    vec_h, pk_h = plan.process(a, b)
+    da = torch.from_numpy(a).cuda()
+    db = torch.from_numpy(b).cuda()
+    dvec = torch.zeros((plan.n, 5), dtype=torch.float32, device="cuda")
+    dpk = torch.zeros(plan.n, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        plan.process_device(da.data_ptr(), db.data_ptr(), 1024, dvec.data_ptr(), dpk.data_ptr(),
+                            s.cuda_stream)
+    s.synchronize()
+    assert np.array_equal(dvec.cpu().numpy(), vec_h)
+    assert np.array_equal(dpk.cpu().numpy(), pk_h)
+
+
+def test_argument_errors():
+    plan = og.Plan(128, 128, np.uint16, 32, 16)
+    a = np.zeros((128, 128), np.uint16)
+    with pytest.raises(og.OpivError) as e:
+        plan.process_into(a.ctypes.data, a.ctypes.data, 100, np.zeros(plan.n * 5, np.float32).ctypes.data, None)
+    assert e.value.status == og.ERR_ARG
+    with pytest.raises(og.OpivError) as e:
+        plan.process(a[:, :64], a[:, :64])
+    assert e.value.status == og.ERR_SIZE_MISMATCH
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(128, 128, np.uint16, 32, 16, device=1 << 20)
+    assert e.value.status == og.ERR_ARG
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(512, 512, np.uint16, 128, 16)
+    assert e.value.status == og.ERR_UNSUPPORTED
