@@ -43,6 +43,14 @@ namespace opiv {
 namespace fp32 {
 
 constexpr int kWarps = 4;   // warps per CTA
+// Certification margins: a window is decided by this kernel only if the
+// error bound of its sub-pixel fit stays below kFitTol pixels and the
+// relative error bound of its sn below kSnTol * (1 + sn).  The parity
+// tolerances are 1e-4 px and 1e-5 * (1 + sn): sn = p0 / p1 is a ratio of
+// plane values, and plane values are specified to 1e-5 of the plane peak p0,
+// which bounds the relative error of p1 by 1e-5 * p0 / p1 = 1e-5 * sn.
+constexpr float kFitTol = 3e-5f;
+constexpr float kSnTol = 3e-6f;
 #define kNegInf (-__int_as_float(0x7f800000))
 
 // Pixel types: 8/16-bit integers are summed exactly (column sums stay below
@@ -341,9 +349,13 @@ piv_fp32_kernel(const PivParams p)
                 float ex, ey;
                 const float fx = gauss_axis(vl, vc, vr, ped, dlt, ex);
                 const float fy = gauss_axis(vu, vc, vd, ped, dlt, ey);
-                const float p1 = t1 + ped;
+                const float p0 = t0 + ped, p1 = t1 + ped;
+                // sn = p0 / p1 when p1 > 0: relative error <= e/|p0| + e/|p1|
+                // with e = dlt / 2 the error of one plane value
+                const float sn_err = 0.5f * dlt * (1.f / fabsf(p0) + 1.f / fabsf(p1));
                 certain = (umax < t1 - 2.f * dlt) && (t0 - t1 > dlt) && (fabsf(p1) > dlt) &&
-                          (ex < 1e-5f) && (ey < 1e-5f);
+                          (ex < kFitTol) && (ey < kFitTol) &&
+                          (p1 <= 0.f || sn_err < kSnTol * (1.f + p0 / p1));
                 int bx, by;
                 window_origin(p, w, bx, by);
                 out.x = (float)(bx + W / 2);
