@@ -124,6 +124,23 @@ int64_t opiv_plan_exact_count(opiv_plan* plan);
 int opiv_plan_set_timing(opiv_plan* plan, int enable);
 int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
 
+/* ---- allocation-free pass ------------------------------------------------ */
+/* No counterpart in the reference.  The same pass as opiv_process_pair_device
+ * for callers that must not allocate device memory once they are running
+ * (fixed-budget acquisition loops, hosts that own the device allocator): no
+ * plan, no cudaMalloc / cudaFree.  Its scratch lives in one fixed device
+ * array of about 4 MiB that every GPU using the library holds until exit.
+ * Grids of more than 1,048,576 windows are rejected (OPIV_ERR_CAPACITY).
+ * The first call on a device does a one-time set-up (address lookup and a
+ * synchronous table upload): make it before any stream capture.  All calls
+ * share the scratch; calls that overlap on the GPU race, so order them on
+ * one stream.  Uses the current device; asynchronous on `stream`. */
+int opiv_process_pair_device_noalloc(const void* d_frame_a, const void* d_frame_b,
+                                     size_t pitch_bytes, uint32_t img_w, uint32_t img_h, int dtype,
+                                     uint32_t ia, uint32_t dx, uint32_t dy, int mode,
+                                     int limit_search, opiv_vector* d_out_vec, int32_t* d_out_peak,
+                                     void* stream);
+
 /* ---- per-window correlation (FFT::cross_correlate[_real] on a batch) ------ */
 /* n window pairs of w x w doubles (a, b: n*w*w each, row-major), planes out:
  * n*w*w doubles, quadrant-swapped as the reference returns them.

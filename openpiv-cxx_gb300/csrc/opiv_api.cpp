@@ -110,6 +110,12 @@ constexpr float kKappa = 8.0f;
 
 }  // namespace
 
+int opiv::record_error(int status, const char* message)
+{
+    g_last_error = message;
+    return status;
+}
+
 struct opiv_plan {
     int device = 0;
     uint32_t img_w = 0, img_h = 0, ia = 0, dx = 0, dy = 0;

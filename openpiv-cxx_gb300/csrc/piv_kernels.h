@@ -57,4 +57,8 @@ bool exact_supports(int w);
 cudaError_t launch_piv_exact(const PivParams& p, int w, int dtype, int mode, int limit,
                              bool use_list, int blocks, cudaStream_t s);
 
+// Records `message` as the calling thread's last error (opiv_last_error)
+// and returns `status`.
+int record_error(int status, const char* message);
+
 }  // namespace opiv

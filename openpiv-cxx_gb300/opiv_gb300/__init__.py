@@ -45,7 +45,7 @@ SYMBOLS = [
     "opiv_plan_window_count", "opiv_plan_grid", "opiv_process_pair",
     "opiv_process_pair_device", "opiv_plan_exact_count", "opiv_plan_set_timing",
     "opiv_plan_last_timing", "opiv_cross_correlate_batch",
-    "opiv_find_peaks", "opiv_fit_simple_gaussian",
+    "opiv_find_peaks", "opiv_fit_simple_gaussian", "opiv_process_pair_device_noalloc",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -101,6 +101,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_plan_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.opiv_cross_correlate_batch.argtypes = [_dp, _dp, C.c_uint32, C.c_int64, C.c_int, C.c_int,
                                              _dp, C.c_int]
+    L.opiv_process_pair_device_noalloc.argtypes = [
+        C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_int, C.c_uint32,
+        C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -213,6 +216,17 @@ class Plan:
         a, b = C.c_float(), C.c_float()
         _check(load().opiv_plan_last_timing(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+# ---- allocation-free pass --------------------------------------------------
+def process_pair_device_noalloc(d_a: int, d_b: int, pitch: int, img_w: int, img_h: int, dtype,
+                                ia: int, dx: int, dy: int, mode: int, limit_search: bool,
+                                d_vec: int, d_peak: int | None, stream: int = 0):
+    """The pass without a plan and without any device allocation (current
+    device, asynchronous on `stream`).  See opiv_process_pair_device_noalloc."""
+    _check(load().opiv_process_pair_device_noalloc(
+        d_a, d_b, pitch, img_w, img_h, DTYPES[np.dtype(dtype)], ia, dx, dy, mode,
+        int(bool(limit_search)), d_vec, d_peak, stream or None))
 
 
 # ---- per-window API --------------------------------------------------------
