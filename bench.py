@@ -113,7 +113,9 @@ class ClockSampler:
                                     if r[3].replace(".", "").isdigit()), default=None)}
 
 
-def dist_setup(args):
+def dist_setup(args=None):
+    """Rank, world size and local rank from the torchrun environment; for
+    N > 1 joins the process group (NCCL with GPUs, gloo without)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -121,18 +123,23 @@ def dist_setup(args):
         import torch
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", init_method="env://")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", init_method="env://")
+        else:
+            dist.init_process_group("gloo", init_method="env://")
     return rank, world, local
 
 
 def dist_max(x: float, world: int) -> float:
+    """Maximum of x over the ranks (the slowest replica's time)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

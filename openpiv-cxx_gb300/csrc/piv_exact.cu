@@ -20,8 +20,8 @@
 //
 // It serves two purposes: it re-decides the windows the FP32 kernel flagged
 // as uncertain, and it is the device FP64 correlation used by the exact
-// per-window API.  One CTA handles one window at a time; CTAs stride over
-// the work list.  FP64 is slow on this part, so the hot path only sends
+// per-window API.  One CTA of 256 threads handles one window at a time;
+// CTAs stride over the work list.  FP64 is slow on this part, so the hot path only sends
 // the rare flagged windows here.
 
 #include <cstdint>
@@ -34,7 +34,7 @@ namespace opiv {
 
 namespace {
 
-constexpr int kThreads = 64;
+constexpr int kThreads = 256;
 constexpr int kMaxW = 64;
 
 __device__ __forceinline__ double2 e_add(double2 a, double2 b)
@@ -58,40 +58,49 @@ __device__ __forceinline__ double px_d(const uint16_t* p) { return (double)__ldg
 __device__ __forceinline__ double px_d(const float* p) { return (double)__ldg(p); }
 __device__ __forceinline__ double px_d(const double* p) { return __ldg(p); }
 
-// In-place radix-2 DIT of n points x[0], x[s], ... (bit-reversal, then
-// butterflies).  tw: table of n entries exp(-+i*pi*j/n).
-__device__ void dit_inplace(double2* x, int n, int s, const double2* tw)
+// Radix-2 DIT transforms of all W lines of a W x W tile, in place, every
+// thread of the block cooperating: rows when (s_line, s_elem) = (W, 1),
+// columns when (1, W).  Per line this is the butterfly graph of fft_inner
+// (bit-reversal, then stages len = 2 .. W combining e + o*w, e - o*w with
+// w = tw[k * 2W/len]); spreading butterflies over threads changes no
+// operation and no operand.  tw: table of W entries exp(-+i*pi*j/W).
+__device__ void dit_lines(double2* X, int W, int lg, int s_line, int s_elem, const double2* tw)
 {
-    int lg = 0;
-    while ((1 << lg) < n) ++lg;
-    for (int i = 0; i < n; ++i) {
+    const int t = threadIdx.x, T = blockDim.x;
+    for (int q = t; q < W * W; q += T) {
+        const int line = q / W, i = q % W;
         const int j = (int)(__brev((unsigned)i) >> (32 - lg));
-        if (lg > 0 && i < j) {
-            const double2 t = x[i * s];
-            x[i * s] = x[j * s];
-            x[j * s] = t;
+        if (i < j) {
+            double2* x = X + line * s_line;
+            const double2 v = x[i * s_elem];
+            x[i * s_elem] = x[j * s_elem];
+            x[j * s_elem] = v;
         }
     }
-    for (int len = 2; len <= n; len <<= 1) {
-        const int half = len >> 1, tstep = (2 * n) / len;
-        for (int base = 0; base < n; base += len) {
-            for (int k = 0; k < half; ++k) {
-                const double2 e = x[(base + k) * s];
-                const double2 o = e_mul(x[(base + k + half) * s], tw[k * tstep]);
-                x[(base + k) * s] = e_add(e, o);
-                x[(base + k + half) * s] = e_sub(e, o);
-            }
+    __syncthreads();
+    const int nb = W / 2;   // butterflies per line and stage
+    for (int len = 2; len <= W; len <<= 1) {
+        const int half = len >> 1, tstep = (2 * W) / len;
+        for (int q = t; q < W * nb; q += T) {
+            const int line = q / nb, b = q % nb;
+            const int base = (b / half) * len, k = b % half;
+            double2* x = X + line * s_line;
+            const double2 e = x[(base + k) * s_elem];
+            const double2 o = e_mul(x[(base + k + half) * s_elem], tw[k * tstep]);
+            x[(base + k) * s_elem] = e_add(e, o);
+            x[(base + k + half) * s_elem] = e_sub(e, o);
         }
+        __syncthreads();
     }
 }
 
+// 2-D transform: every row, then every column (fft.h:104-116).
 __device__ void fft2d(double2* X, int W, const double2* tw)
 {
-    const int t = threadIdx.x;
-    if (t < W) dit_inplace(X + t * W, W, 1, tw);    // rows
-    __syncthreads();
-    if (t < W) dit_inplace(X + t, W, W, tw);        // columns
-    __syncthreads();
+    int lg = 0;
+    while ((1 << lg) < W) ++lg;
+    dit_lines(X, W, lg, W, 1, tw);
+    dit_lines(X, W, lg, 1, W, tw);
 }
 
 __device__ __forceinline__ void window_origin(const PivParams& p, int64_t w, int& bx, int& by)

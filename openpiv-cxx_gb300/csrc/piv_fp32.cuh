@@ -1,37 +1,43 @@
 // piv_fp32.cuh -- fused FP32 PIV window kernel for sm_103a (template; the
 // piv_fp32_w*.cu files instantiate it per window size).
 //
-// One warp processes a task of 2*NG interrogation windows (NG = 32/W lane
-// groups of W lanes; W = 32 -> one group, W = 16 -> two groups).  Per window:
+// A warp processes a task of 2*NG interrogation windows: NG = 32/W lane
+// groups of W lanes, each group a pair of windows.  Per window:
 //
-//   extract (core::extract, image_utils.impl.h:392-419), widen to float and
-//   subtract the window mean; z = a + i*b;
-//   2-D FFT of z in registers: column FFT (lane = column), transpose through
-//   a swizzled shared-memory tile, row FFT;
-//   two-for-one unpack A = (Z[k] + conj Z[-k])/2, B = (Z[k] - conj Z[-k])/2i
-//   via a lane shuffle, product P = B * conj(A) (fft.h:188-227), with the
-//   reference's zeroed spectrum row 0, row W/2 and column 0 in REAL mode;
-//   the products of two windows are packed as Q = P1 + i*P2 (both are
-//   Hermitian, so one complex inverse gives both real planes);
-//   inverse row FFT, transpose, inverse column FFT -> both planes;
+//   extract (core::extract, image_utils.impl.h:392-419): lane = window row,
+//   128-bit loads where the grid is 16-byte aligned, pixels widened to float
+//   exactly (byte-permute into the mantissa of 2^23, then subtract 2^23);
+//   z = a + i*b (join_from_channels, image_utils.impl.h:294-315);
+//   2-D FFT of z in registers: row FFT (lane = row), transpose through a
+//   padded shared-memory tile, column FFT;
+//   the two-for-one unpack and the product in one step: with Zm = Z[-k]
+//   (fetched from the mirror lane by a shuffle),
+//       P = B conj(A) = ( Im(Z Zm) / 2 , (|Zm|^2 - |Z|^2) / 4 ),
+//   which is FFT(b) conj(FFT(a)) of fft.h:188-227; REAL mode leaves the
+//   reference's unpacked set only (fft.h:166-183: spectrum row 0, row W/2
+//   and column 0 stay zero), done by zeroing those Z rows / the Z column;
+//   the products of the pair are packed as Q = conj(P1) + i conj(P2): both
+//   P are Hermitian, so one *forward* 2-D FFT of Q gives plane1 + i plane2
+//   (the reference's unnormalised inverse, fft.h:223, up to the shared
+//   conjugation);
 //   quadrant swap as an index remap (swap_quadrants, impl:367-386);
-//   find_peaks(plane, 2, 1) (impl:42-74) as a warp scan + top-2 reduction
-//   (ties to the lowest row-major index, the order the reference's sort
-//   keeps among equal values);
+//   find_peaks(plane, 2, 1) (impl:42-74): warp scan + top-2 reduction;
 //   fit_simple_gaussian (impl:77-101) and the vector of main.cpp:220-236.
 //
-// Mean subtraction changes only the DC bin; the kernel zeroes that bin and
-// adds the exact pedestal (sum a)(sum b) back where values are used, which
-// is the reference's raw (unsubtracted) plane.  Planes are computed 4x
-// scaled (the 1/2 factors of the unpack are dropped); ratios are unaffected
-// and the pedestal is scaled to match.
+// Every 1-D transform is the same in-register radix-2 DIF routine, run from
+// one runtime loop over the six transform stages of a pair, so the kernel's
+// code stays small enough for the instruction caches.
 //
-// Every window gets a certification test: decisions (local-max tests, the
-// order of the two peaks, signs entering log and sn, the conditioning of
-// the Gaussian fit) whose margin is below an error bound of the FP32 plane
-// are flagged; flagged windows are re-evaluated by the exact double
-// precision kernel (piv_exact.cu), which overwrites their results.
-
+// The DC product is dropped (P[0][0] = 0) and the pedestal (sum a)(sum b),
+// read from the DC bin of Z, is added back where plane values are used:
+// the plane then is the reference's raw plane.  Values are 4x scaled; ratios
+// are unaffected and the pedestal is scaled to match.
+//
+// Certification: decisions whose margin is below an error bound of the
+// FP32 plane (local-max tests, order of the two peaks, signs entering log
+// and sn, conditioning of the fit and of sn) flag the window; flagged
+// windows are re-decided by the exact double-precision kernel
+// (piv_exact.cu), which overwrites their results.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -43,31 +49,74 @@ namespace opiv {
 namespace fp32 {
 
 constexpr int kWarps = 4;   // warps per CTA
-// Certification margins: a window is decided by this kernel only if the
-// error bound of its sub-pixel fit stays below kFitTol pixels and the
-// relative error bound of its sn below kSnTol * (1 + sn).  The parity
-// tolerances are 1e-4 px and 1e-5 * (1 + sn): sn = p0 / p1 is a ratio of
-// plane values, and plane values are specified to 1e-5 of the plane peak p0,
-// which bounds the relative error of p1 by 1e-5 * p0 / p1 = 1e-5 * sn.
+// A window is decided by this kernel only if the error bound of its
+// sub-pixel fit stays below kFitTol pixels and the relative error bound of
+// its sn below kSnTol * (1 + sn).  The parity tolerances are 1e-4 px and
+// 1e-5 * (1 + sn): sn = p0 / p1 is a ratio of plane values, and plane values
+// are specified to 1e-5 of the plane peak p0, which bounds the relative
+// error of p1 by 1e-5 * p0 / p1 = 1e-5 * sn.
 constexpr float kFitTol = 3e-5f;
 constexpr float kSnTol = 3e-6f;
 #define kNegInf (-__int_as_float(0x7f800000))
+constexpr float kTwo23 = 8388608.0f;
 
-// Pixel types: 8/16-bit integers are summed exactly (column sums stay below
-// 2^24, window sums in int); float frames are summed in float; double input
-// (the per-window batch API) is summed in double.
-template <typename PixT> struct px_traits {
-    using acc = float;
-    static constexpr bool integer = true;
-};
-template <> struct px_traits<float> {
-    using acc = float;
-    static constexpr bool integer = false;
-};
-template <> struct px_traits<double> {
-    using acc = double;
-    static constexpr bool integer = false;
-};
+// ---- pixel loading -----------------------------------------------------------
+// Exact widening of 8/16-bit pixels: bits 0x4B000000 | u are the float
+// 2^23 + u (u < 2^23); subtracting 2^23 is exact.
+__device__ __forceinline__ float u16_lo(uint32_t w) { return __int_as_float(__byte_perm(w, 0x4B00, 0x5410)) - kTwo23; }
+__device__ __forceinline__ float u16_hi(uint32_t w) { return __int_as_float(__byte_perm(w, 0x4B00, 0x5432)) - kTwo23; }
+template <int K>
+__device__ __forceinline__ float u8_k(uint32_t w) { return __int_as_float(__byte_perm(w, 0x4B00, 0x5440 | K)) - kTwo23; }
+
+// W consecutive pixels starting at `ptr` into the x (A) or y (B) components
+// of v.  VEC: the row start is 16-byte aligned.
+template <bool B>
+__device__ __forceinline__ void put(float2& z, float f)
+{
+    if (B) z.y = f;
+    else z.x = f;
+}
+
+template <int W, bool B, typename PixT, bool VEC>
+__device__ __forceinline__ void load_row(const PixT* ptr, float2 (&v)[W])
+{
+    if (VEC && sizeof(PixT) == 2) {
+        const uint4* q = reinterpret_cast<const uint4*>(ptr);
+#pragma unroll
+        for (int k = 0; k < W / 8; ++k) {
+            const uint4 r = __ldg(q + k);
+            put<B>(v[8 * k + 0], u16_lo(r.x)); put<B>(v[8 * k + 1], u16_hi(r.x));
+            put<B>(v[8 * k + 2], u16_lo(r.y)); put<B>(v[8 * k + 3], u16_hi(r.y));
+            put<B>(v[8 * k + 4], u16_lo(r.z)); put<B>(v[8 * k + 5], u16_hi(r.z));
+            put<B>(v[8 * k + 6], u16_lo(r.w)); put<B>(v[8 * k + 7], u16_hi(r.w));
+        }
+    } else if (VEC && sizeof(PixT) == 1) {
+        const uint4* q = reinterpret_cast<const uint4*>(ptr);
+#pragma unroll
+        for (int k = 0; k < W / 16; ++k) {
+            const uint4 r = __ldg(q + k);
+            const uint32_t w4[4] = { r.x, r.y, r.z, r.w };
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                put<B>(v[16 * k + 4 * j + 0], u8_k<0>(w4[j]));
+                put<B>(v[16 * k + 4 * j + 1], u8_k<1>(w4[j]));
+                put<B>(v[16 * k + 4 * j + 2], u8_k<2>(w4[j]));
+                put<B>(v[16 * k + 4 * j + 3], u8_k<3>(w4[j]));
+            }
+        }
+    } else if (VEC && sizeof(PixT) == 4) {
+        const float4* q = reinterpret_cast<const float4*>(ptr);
+#pragma unroll
+        for (int k = 0; k < W / 4; ++k) {
+            const float4 r = __ldg(q + k);
+            put<B>(v[4 * k + 0], r.x); put<B>(v[4 * k + 1], r.y);
+            put<B>(v[4 * k + 2], r.z); put<B>(v[4 * k + 3], r.w);
+        }
+    } else {
+#pragma unroll
+        for (int x = 0; x < W; ++x) put<B>(v[x], (float)__ldg(ptr + x));
+    }
+}
 
 __device__ __forceinline__ void window_origin(const PivParams& p, int64_t w, int& bx, int& by)
 {
@@ -81,21 +130,8 @@ __device__ __forceinline__ void window_origin(const PivParams& p, int64_t w, int
     }
 }
 
-// swizzled W x W tile: element (r, c) at r*W + (c ^ r); conflict-free for
-// row-wise and column-wise float2 access by W lanes.
-template <int W>
-__device__ __forceinline__ int swz(int r, int c) { return r * W + (c ^ r); }
-
-// sum over the W lanes of a group
-template <int W, typename T = float>
+template <int W, typename T>
 __device__ __forceinline__ T group_sum(T x)
-{
-#pragma unroll
-    for (int o = W / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o, W);
-    return x;
-}
-template <int W>
-__device__ __forceinline__ int group_sum_int(int x)
 {
 #pragma unroll
     for (int o = W / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o, W);
@@ -109,33 +145,15 @@ __device__ __forceinline__ float group_max(float x)
     return x;
 }
 
-// One axis of the 3-point Gaussian fit on pedestal-shifted values
-// L = l + ped, C = c + ped, R = r + ped (ped added implicitly):
-//   (ln L - ln R) / (2 (ln L + ln R - 2 ln C)),  0 if the denominator is 0,
-// NaN if any of L, C, R <= 0 (the reference takes log of a non-positive
-// number there).  Also returns a bound on the error caused by an absolute
-// error `dlt` in each of the plane values.
-__device__ __forceinline__ float gauss_axis(float l, float c, float r, float ped, float dlt,
-                                            float& err)
-{
-    const float L = l + ped, C = c + ped, R = r + ped;
-    if (!(L > 0.f && C > 0.f && R > 0.f)) {
-        err = 0.f;
-        return __int_as_float(0x7fffffff);
-    }
-    const float num = log1pf((l - r) / R);
-    const float den = log1pf((l - c) / C) + log1pf((r - c) / C);
-    if (den == 0.f) {
-        err = 3.4e38f;   // degenerate: leave it to the exact pass
-        return 0.f;
-    }
-    const float f = num / (2.f * den);
-    const float m = fminf(fminf(L, R), C);
-    err = dlt * (1.f + 4.f * fabsf(f)) / (m * 2.f * fabsf(den));
-    return f;
-}
+// W x W tile with rows padded to W + 1 float2: row-wise and column-wise
+// accesses by the W lanes of a group hit distinct banks.
+template <int W>
+__device__ __forceinline__ int tix(int r, int c) { return r * (W + 1) + c; }
 
-template <int W, int MODE, bool LIMIT, typename PixT, bool PLANES>
+// Transform stages of a pair, run by one runtime loop around one FFT body.
+enum { kStLoad0 = 0, kStCol0 = 1, kStLoad1 = 2, kStCol1 = 3, kStInvA = 4, kStInvB = 5 };
+
+template <int W, int MODE, bool LIMIT, typename PixT, bool PLANES, bool VEC>
 __global__ void __launch_bounds__(32 * kWarps, (W == 32 ? 3 : 4))
 piv_fp32_kernel(const PivParams p)
 {
@@ -148,7 +166,7 @@ piv_fp32_kernel(const PivParams p)
     constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
 
-    __shared__ float2 smem[kWarps][NG][N];
+    __shared__ float2 smem[kWarps][NG][W * (W + 1)];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -163,113 +181,116 @@ piv_fp32_kernel(const PivParams p)
     const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
     const size_t pitch = p.pitch / sizeof(PixT);
 
-    float2 P[W];
-    // per-window values of the two windows this group handles (scalars, so
-    // that they stay in registers across the runtime loop)
-    float ped4_0 = 0.f, ped4_1 = 0.f, en_0 = 0.f, en_1 = 0.f;
+    float2 v[W];      // the transform being worked on
+    float2 Q[W];      // conj(P1) + i conj(P2), lane = kx, register i <-> ky = bitrev(i)
+    float en0 = 0.f, en1 = 0.f, ped0 = 0.f, ped1 = 0.f;
 
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
+    for (int st = 0; st < 6; ++st) {
+        const int h = (st >= kStLoad1 && st <= kStCol1) ? 1 : 0;
         const int64_t w = first + h * NG + grp;
         const bool valid = w < p.n_win;
-        int bx = 0, by = 0;
-        if (valid) window_origin(p, w, bx, by);
-
-        // ---- extract + widen (lane = column x, register = row y)
-        using acc_t = typename px_traits<PixT>::acc;
-        float2 v[W];
-        acc_t ca = 0, cb = 0;
-        if (valid) {
-            const PixT* ra = fa + (size_t)by * pitch + bx + gl;
-            const PixT* rb = fb + (size_t)by * pitch + bx + gl;
-#pragma unroll
-            for (int y = 0; y < W; ++y) {
-                const acc_t pa = (acc_t)__ldg(ra + (size_t)y * pitch);
-                const acc_t pb = (acc_t)__ldg(rb + (size_t)y * pitch);
-                v[y].x = (float)pa;
-                v[y].y = (float)pb;
-                ca += pa;
-                cb += pb;
-            }
-        } else {
-#pragma unroll
-            for (int y = 0; y < W; ++y) v[y] = make_float2(0.f, 0.f);
-        }
-        float sa, sb;
-        double dped;                    // (sum a)(sum b), exact for integer pixels
-        if (px_traits<PixT>::integer) { // column sums are exact integers < 2^24
-            const int isa = group_sum_int<W>((int)ca);
-            const int isb = group_sum_int<W>((int)cb);
-            sa = (float)isa;
-            sb = (float)isb;
-            dped = PLANES ? (double)isa * (double)isb : 0.0;
-        } else {
-            const acc_t ta = group_sum<W, acc_t>(ca);
-            const acc_t tb = group_sum<W, acc_t>(cb);
-            sa = (float)ta;
-            sb = (float)tb;
-            dped = PLANES ? (double)ta * (double)tb : 0.0;
-        }
-        const float ma = sa * (1.f / N), mb = sb * (1.f / N);
-        float e = 0.f;
-#pragma unroll
-        for (int y = 0; y < W; ++y) {
-            v[y].x -= ma;
-            v[y].y -= mb;
-            e = fmaf(v[y].x, v[y].x, e);
-            e = fmaf(v[y].y, v[y].y, e);
-        }
-        e = group_sum<W>(e);
-        const float pd = (MODE == kModeComplex) ? 4.f * sa * sb : 0.f;
-        if (h == 0) { en_0 = e; ped4_0 = pd; } else { en_1 = e; ped4_1 = pd; }
-        if (PLANES && valid && gl == 0)
-            p.peds[w] = (MODE == kModeComplex) ? dped : 0.0;
-
-        // ---- forward 2-D FFT
-        fft_dif<W, false>(v);                       // columns: v[i] = Zc[bitrev(i)][gl]
-#pragma unroll
-        for (int i = 0; i < W; ++i) S[swz<W>(bitrev<W>(i), gl)] = v[i];
-        __syncwarp();
-#pragma unroll
-        for (int j = 0; j < W; ++j) v[j] = S[swz<W>(gl, j)];
-        __syncwarp();
-        fft_dif<W, false>(v);                       // rows: v[i] = Z[ky = gl][kx = bitrev(i)]
-
-        // ---- unpack and conjugate product
-        const int pl = (W - gl) & (W - 1);
-        const bool zero_row = (MODE == kModeReal) && (gl == 0 || gl == W / 2);
-#pragma unroll
-        for (int i = 0; i < W; ++i) {
-            const int kx = bitrev<W>(i);
-            const int mi = bitrev<W>((W - kx) & (W - 1));
-            float2 zm;
-            zm.x = __shfl_sync(0xffffffffu, v[mi].x, pl, W);
-            zm.y = __shfl_sync(0xffffffffu, v[mi].y, pl, W);
-            const float2 z = v[i];
-            const float2 a2 = make_float2(z.x + zm.x, z.y - zm.y);   // 2 A
-            const float2 b2 = make_float2(z.y + zm.y, zm.x - z.x);   // 2 B
-            float2 q = make_float2(b2.x * a2.x + b2.y * a2.y, b2.y * a2.x - b2.x * a2.y);
-            bool zero = zero_row || (MODE == kModeReal && kx == 0) || (kx == 0 && gl == 0);
-            if (zero) q = make_float2(0.f, 0.f);
-            if (h == 0) {
-                P[i] = q;
+        // ---------------- before the transform
+        if (st == kStLoad0 || st == kStLoad1) {
+            // extract + widen: lane = row y, registers = x
+            if (valid) {
+                int bx, by;
+                window_origin(p, w, bx, by);
+                const size_t off = (size_t)(by + gl) * pitch + bx;
+                load_row<W, false, PixT, VEC>(fa + off, v);
+                load_row<W, true, PixT, VEC>(fb + off, v);
             } else {
-                P[i] = make_float2(P[i].x - q.y, P[i].y + q.x);
+#pragma unroll
+                for (int x = 0; x < W; ++x) v[x] = make_float2(0.f, 0.f);
+            }
+            float e = 0.f;
+#pragma unroll
+            for (int x = 0; x < W; ++x) e = fmaf(v[x].x, v[x].x, fmaf(v[x].y, v[x].y, e));
+            e = group_sum<W, float>(e);
+            if (h == 0) en0 = e; else en1 = e;
+            if (PLANES && valid) {   // exact pedestal for the per-window API (double input)
+                double sa = 0.0, sb = 0.0;
+                const double* da = reinterpret_cast<const double*>(fa);
+                const double* db = reinterpret_cast<const double*>(fb);
+                int bx, by;
+                window_origin(p, w, bx, by);
+#pragma unroll 4
+                for (int x = 0; x < W; ++x) {
+                    sa += da[(size_t)(by + gl) * pitch + bx + x];
+                    sb += db[(size_t)(by + gl) * pitch + bx + x];
+                }
+                sa = group_sum<W, double>(sa);
+                sb = group_sum<W, double>(sb);
+                if (gl == 0) p.peds[w] = (MODE == kModeComplex) ? sa * sb : 0.0;
+            }
+        } else if (st == kStCol0 || st == kStCol1) {
+            // v: lane = y, register i <-> kx = bitrev(i).  Transpose to
+            // lane = kx, registers = y.  REAL mode: column kx = 0 of Z is
+            // zeroed here (register 0), so lane 0's spectrum is zero.
+#pragma unroll
+            for (int i = 0; i < W; ++i) {
+                const float2 z = (MODE == kModeReal && i == 0) ? make_float2(0.f, 0.f) : v[i];
+                S[tix<W>(bitrev<W>(i), gl)] = z;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int y = 0; y < W; ++y) v[y] = S[tix<W>(gl, y)];
+            __syncwarp();
+        } else if (st == kStInvA) {
+            // Q: lane = kx, register i <-> ky = bitrev(i).  To lane = ky,
+            // registers = kx.
+#pragma unroll
+            for (int i = 0; i < W; ++i) S[tix<W>(bitrev<W>(i), gl)] = Q[i];
+            __syncwarp();
+#pragma unroll
+            for (int x = 0; x < W; ++x) v[x] = S[tix<W>(gl, x)];
+            __syncwarp();
+        } else {   // kStInvB
+            // v: lane = ky, register i <-> x = bitrev(i).  To lane = x,
+            // registers = ky.
+#pragma unroll
+            for (int i = 0; i < W; ++i) S[tix<W>(bitrev<W>(i), gl)] = v[i];
+            __syncwarp();
+#pragma unroll
+            for (int y = 0; y < W; ++y) v[y] = S[tix<W>(gl, y)];
+            __syncwarp();
+        }
+
+        fft_dif<W, false>(v);
+
+        // ---------------- after the transform
+        if (st == kStCol0 || st == kStCol1) {
+            // v: lane = kx, register i <-> ky = bitrev(i).  DC bin = (sum a,
+            // sum b) on lane 0, register 0.
+            const float2 dc = make_float2(__shfl_sync(0xffffffffu, v[0].x, 0, W),
+                                          __shfl_sync(0xffffffffu, v[0].y, 0, W));
+            const float pd = (MODE == kModeComplex) ? 4.f * dc.x * dc.y : 0.f;
+            if (h == 0) ped0 = pd; else ped1 = pd;
+            if (MODE == kModeComplex && gl == 0) v[0] = make_float2(0.f, 0.f);
+            if (MODE == kModeReal) {   // rows ky = 0 and ky = W/2
+                v[0] = make_float2(0.f, 0.f);
+                v[1] = make_float2(0.f, 0.f);
+            }
+            const int pl = (W - gl) & (W - 1);
+#pragma unroll
+            for (int i = 0; i < W; ++i) {
+                const int ky = bitrev<W>(i);
+                const int mi = bitrev<W>((W - ky) & (W - 1));
+                const float2 z = v[i];
+                const float zmx = __shfl_sync(0xffffffffu, v[mi].x, pl, W);
+                const float zmy = __shfl_sync(0xffffffffu, v[mi].y, pl, W);
+                // 4 conj(P) = ( 2 Im(Z Zm), |Z|^2 - |Zm|^2 )
+                const float im2 = 2.f * fmaf(z.x, zmy, z.y * zmx);
+                const float d = fmaf(z.x, z.x, fmaf(z.y, z.y, -fmaf(zmx, zmx, zmy * zmy)));
+                if (h == 0) Q[i] = make_float2(im2, d);
+                else Q[i] = make_float2(Q[i].x - d, Q[i].y + im2);
             }
         }
     }
+    // v: lane = x, register i <-> y = bitrev(i); v.x = plane of the first
+    // window of the pair, v.y of the second (4x scaled, pedestal removed).
 
-    // ---- inverse 2-D FFT of Q = P1 + i P2
-    fft_dit<W, true>(P);                            // rows: P[j] = R[ky = gl][x = j]
-#pragma unroll
-    for (int j = 0; j < W; ++j) S[swz<W>(gl, j)] = P[j];
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < W; ++i) P[i] = S[swz<W>(bitrev<W>(i), gl)];
-    __syncwarp();
-    fft_dit<W, true>(P);                            // columns: P[y] = corr[y][x = gl]
-
-    const float dlt = p.kappa * 5.9604645e-8f * 2.f * (float)N * (en_0 + en_1);
+    const float dlt = p.kappa * 5.9604645e-8f * 2.f * (float)N * (en0 + en1);
     const int xs = (gl + W / 2) & (W - 1);          // swapped column of this lane
     const bool col_ok = xs >= SX0 && xs < SX1;
 
@@ -277,15 +298,18 @@ piv_fp32_kernel(const PivParams p)
     for (int h = 0; h < 2; ++h) {
         const int64_t w = first + h * NG + grp;
         const bool valid = w < p.n_win;
-        float val[W];
+        float val[W];                                // val[i] <-> y = bitrev(i)
 #pragma unroll
-        for (int y = 0; y < W; ++y) val[y] = h ? P[y].y : P[y].x;
+        for (int i = 0; i < W; ++i) val[i] = h ? v[i].y : v[i].x;
 
+        // plane rows y into shared memory (row-major, padded) for the fit
+#pragma unroll
+        for (int i = 0; i < W; ++i) S[tix<W>(bitrev<W>(i), gl)] = make_float2(val[i], 0.f);
         if (PLANES && valid) {
 #pragma unroll
-            for (int y = 0; y < W; ++y) {
-                const int ys = (y + W / 2) & (W - 1);
-                p.planes[(size_t)w * N + ys * W + xs] = 0.25f * val[y];
+            for (int i = 0; i < W; ++i) {
+                const int ys = (bitrev<W>(i) + W / 2) & (W - 1);
+                p.planes[(size_t)w * N + ys * W + xs] = 0.25f * val[i];
             }
         }
 
@@ -295,14 +319,14 @@ piv_fp32_kernel(const PivParams p)
 #pragma unroll
         for (int ys = SY0; ys < SY1; ++ys) {
             const int y = (ys + W / 2) & (W - 1);
-            const float c = val[y];
-            const float up = val[(y + W - 1) & (W - 1)];
-            const float dn = val[(y + 1) & (W - 1)];
+            const float c = val[bitrev<W>(y)];
+            const float up = val[bitrev<W>((y + W - 1) & (W - 1))];
+            const float dn = val[bitrev<W>((y + 1) & (W - 1))];
             const float lf = __shfl_sync(0xffffffffu, c, (gl + W - 1) & (W - 1), W);
             const float rt = __shfl_sync(0xffffffffu, c, (gl + 1) & (W - 1), W);
-            const float m = fmaxf(fmaxf(up, dn), fmaxf(lf, rt));
-            const bool strict = col_ok && (m < c);
-            const bool unc = col_ok && (fabsf(m - c) <= dlt);
+            const float dd = fmaxf(fmaxf(up, dn), fmaxf(lf, rt)) - c;
+            const bool strict = col_ok && (dd < 0.f);
+            const bool unc = col_ok && (fabsf(dd) <= dlt);
             umax = unc ? fmaxf(umax, c) : umax;
             const float sv = strict ? c : kNegInf;
             const bool gt = sv > t0;
@@ -323,32 +347,57 @@ piv_fp32_kernel(const PivParams p)
             t1 = n1;
         }
         umax = group_max<W>(umax);
-
-        // ---- neighbourhood of the first peak (through shared memory)
-#pragma unroll
-        for (int y = 0; y < W; ++y) S[y * W + gl] = make_float2(val[y], 0.f);
         __syncwarp();
+
+        // ---- fit_simple_gaussian: the six logarithms on six lanes
         const int px = key % W, py = key / W;       // swapped-plane coordinates
         const int ux = (px + W / 2) & (W - 1), uy = (py + W / 2) & (W - 1);
-        const float vc = S[uy * W + ux].x;
-        const float vl = S[uy * W + ((ux + W - 1) & (W - 1))].x;
-        const float vr = S[uy * W + ((ux + 1) & (W - 1))].x;
-        const float vu = S[((uy + W - 1) & (W - 1)) * W + ux].x;
-        const float vd = S[((uy + 1) & (W - 1)) * W + ux].x;
+        const float ped = h ? ped1 : ped0;
+        const float vc = S[tix<W>(uy, ux)].x;
+        const float vl = S[tix<W>(uy, (ux + W - 1) & (W - 1))].x;
+        const float vr = S[tix<W>(uy, (ux + 1) & (W - 1))].x;
+        const float vu = S[tix<W>((uy + W - 1) & (W - 1), ux)].x;
+        const float vd = S[tix<W>((uy + 1) & (W - 1), ux)].x;
         __syncwarp();
+        // axis x: ln(L/R), ln(L/C), ln(R/C); axis y: ln(U/D), ln(U/C), ln(D/C)
+        // with L = vl + ped etc., each as log1p((num - den) / (den + ped))
+        const int j = gl < 6 ? gl : 0;
+        const float an = j == 0 ? vl : j == 1 ? vl : j == 2 ? vr : j == 3 ? vu : j == 4 ? vu : vd;
+        const float ad = j == 0 ? vr : j == 1 ? vc : j == 2 ? vc : j == 3 ? vd : vc;
+        const float lg = log1pf((an - ad) / (ad + ped));
+        const float lxr = __shfl_sync(0xffffffffu, lg, 0, W);
+        const float lxl = __shfl_sync(0xffffffffu, lg, 1, W);
+        const float lxrr = __shfl_sync(0xffffffffu, lg, 2, W);
+        const float lyd = __shfl_sync(0xffffffffu, lg, 3, W);
+        const float lyu = __shfl_sync(0xffffffffu, lg, 4, W);
+        const float lydd = __shfl_sync(0xffffffffu, lg, 5, W);
 
         if (valid && gl == 0) {
             const bool has2 = t1 > kNegInf;
-            const float ped = h ? ped4_1 : ped4_0;
             bool certain;
             opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
             int32_t code = -1;
             if (!has2) {
                 certain = !(umax > kNegInf);
             } else {
-                float ex, ey;
-                const float fx = gauss_axis(vl, vc, vr, ped, dlt, ex);
-                const float fy = gauss_axis(vu, vc, vd, ped, dlt, ey);
+                const float C = vc + ped, L = vl + ped, R = vr + ped, U = vu + ped, D = vd + ped;
+                const float nan = __int_as_float(0x7fffffff);
+                // (ln L - ln R) / (2 (ln L + ln R - 2 ln C)), NaN where the
+                // reference takes the log of a non-positive value
+                const float denx = lxl + lxrr, deny = lyu + lydd;
+                const bool okx = L > 0.f && C > 0.f && R > 0.f;
+                const bool oky = U > 0.f && C > 0.f && D > 0.f;
+                const float fx = okx ? lxr / (2.f * denx) : nan;
+                const float fy = oky ? lyd / (2.f * deny) : nan;
+                // error bound of each axis for an error dlt/2 per value; a
+                // NaN outcome is certain only if a value is clearly negative
+                const float mx = fminf(fminf(L, R), C), my = fminf(fminf(U, D), C);
+                const float ex = okx ? (denx == 0.f ? 3.4e38f
+                                        : dlt * (1.f + 4.f * fabsf(fx)) / (mx * 2.f * fabsf(denx)))
+                                     : (mx < -dlt ? 0.f : 3.4e38f);
+                const float ey = oky ? (deny == 0.f ? 3.4e38f
+                                        : dlt * (1.f + 4.f * fabsf(fy)) / (my * 2.f * fabsf(deny)))
+                                     : (my < -dlt ? 0.f : 3.4e38f);
                 const float p0 = t0 + ped, p1 = t1 + ped;
                 // sn = p0 / p1 when p1 > 0: relative error <= e/|p0| + e/|p1|
                 // with e = dlt / 2 the error of one plane value
@@ -362,7 +411,7 @@ piv_fp32_kernel(const PivParams p)
                 out.y = (float)(p.img_h - (by + W / 2));
                 out.u = (float)(W / 2 - px) - fx;
                 out.v = (float)(W / 2 - py) - fy;
-                out.sn = (p1 > 0.f) ? (t0 + ped) / p1 : 0.f;
+                out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
                 code = key;
             }
             p.out_vec[w] = out;
@@ -381,7 +430,16 @@ cudaError_t launch_t(const PivParams& p, cudaStream_t s)
     constexpr int NG = 32 / W;
     const int64_t tasks = (p.n_win + 2 * NG - 1) / (2 * NG);
     const int64_t blocks = (tasks + kWarps - 1) / kWarps;
-    piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES><<<(unsigned)blocks, 32 * kWarps, 0, s>>>(p);
+    const size_t px = sizeof(PixT);
+    // 128-bit loads when every window row starts on a 16-byte boundary
+    const bool vec = p.win_xy == nullptr && ((uintptr_t)p.fa % 16 == 0) &&
+                     ((uintptr_t)p.fb % 16 == 0) && (p.pitch % 16 == 0) &&
+                     (((size_t)p.gx0 * px) % 16 == 0) && (((size_t)p.gdx * px) % 16 == 0) &&
+                     ((W * px) % 16 == 0);
+    if (vec)
+        piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, true><<<(unsigned)blocks, 32 * kWarps, 0, s>>>(p);
+    else
+        piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, false><<<(unsigned)blocks, 32 * kWarps, 0, s>>>(p);
     return cudaGetLastError();
 }
 
