@@ -149,6 +149,89 @@ __device__ __forceinline__ void fft_dit(float2 (&v)[N])
     }
 }
 
+// ---------------------------------------------------------------------------
+// Decimation in time in fused multiply-add form: with w = wx + i wy and
+// t = wy / wx, w*b = wx * (b + i t b), so a +- w*b costs 2 FMAs for
+// c = b + i t b and 4 FMAs for a +- wx*c: 6 instructions per twiddled
+// butterfly instead of 8.  The factor with the larger magnitude is pulled
+// out (wx when |wx| >= |wy|, else wy with w*b = wy * ((wx/wy) b + i b)), which
+// keeps the ratio within [-1, 1].  Tables are evaluated at compile time.
+struct FmaTwiddles {
+    float m[kTwMax];      // pulled-out factor: wx or wy of exp(-2 pi i k / 64)
+    float r[kTwMax];      // ratio: wy / wx or wx / wy
+    bool by_cos[kTwMax];  // |wx| >= |wy|
+};
+
+__host__ __device__ constexpr bool fma_by_cos(int k)
+{
+    // |cos| >= |sin| for angles within 45 degrees of the real axis
+    const int q = k & (kTwMax / 2 - 1);   // k mod 32 (period pi for |cos|, |sin|)
+    return q <= kTwMax / 8 || q >= 3 * kTwMax / 8;
+}
+
+constexpr FmaTwiddles make_fma_twiddles()
+{
+    FmaTwiddles t{};
+    for (int k = 0; k < kTwMax; ++k) {
+        double c = 0, s = 0;
+        cis_2pi(k, kTwMax, c, s);
+        const double wx = c, wy = -s;   // forward twiddle exp(-2 pi i k / 64)
+        const bool bc = fma_by_cos(k);
+        t.by_cos[k] = bc;
+        t.m[k] = (float)(bc ? wx : wy);
+        t.r[k] = (float)(bc ? wy / wx : wx / wy);
+    }
+    return t;
+}
+
+static __constant__ FmaTwiddles c_fma = make_fma_twiddles();
+
+// a, b -> a + w b, a - w b with w = exp(-+2 pi i k / N)
+template <int N, bool INV>
+__device__ __forceinline__ void bfly_dit(float2& a, float2& b, int k)
+{
+    k &= (N - 1);
+    if (k == 0) {
+        const float2 t = b;
+        b = csub(a, t);
+        a = cadd(a, t);
+        return;
+    }
+    if (4 * k == N) {   // w = -i (forward) or i (inverse)
+        const float2 wb = INV ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
+        b = csub(a, wb);
+        a = cadd(a, wb);
+        return;
+    }
+    const int q = k * (kTwMax / N);
+    const float m = (INV && !fma_by_cos(q)) ? -c_fma.m[q] : c_fma.m[q];
+    const float r = INV ? -c_fma.r[q] : c_fma.r[q];
+    float2 c;
+    if (fma_by_cos(q)) {    // w b = wx (bx - t by, by + t bx), t = wy / wx
+        c = make_float2(fmaf(-r, b.y, b.x), fmaf(r, b.x, b.y));
+    } else {                // w b = wy (s bx - by, s by + bx), s = wx / wy
+        c = make_float2(fmaf(r, b.x, -b.y), fmaf(r, b.y, b.x));
+    }
+    b = make_float2(fmaf(-m, c.x, a.x), fmaf(-m, c.y, a.y));
+    a = make_float2(fmaf(m, c.x, a.x), fmaf(m, c.y, a.y));
+}
+
+// Decimation in time, FMA form: bit-reversed input (v[i] holds
+// x[bitrev(i)]), natural-order output.
+template <int N, bool INV>
+__device__ __forceinline__ void fft_dit_fma(float2 (&v)[N])
+{
+#pragma unroll
+    for (int half = 1; half < N; half <<= 1) {
+#pragma unroll
+        for (int base = 0; base < N; base += 2 * half) {
+#pragma unroll
+            for (int j = 0; j < half; ++j)
+                bfly_dit<N, INV>(v[base + j], v[base + j + half], j * (N / (2 * half)));
+        }
+    }
+}
+
 template <int N>
 __host__ __device__ constexpr int bitrev(int i)
 {

@@ -24,7 +24,8 @@
 //   find_peaks(plane, 2, 1) (impl:42-74): warp scan + top-2 reduction;
 //   fit_simple_gaussian (impl:77-101) and the vector of main.cpp:220-236.
 //
-// Every 1-D transform is the same in-register radix-2 DIF routine, run from
+// Every 1-D transform is the same in-register radix-2 DIT routine (FMA form,
+// fft_reg.cuh), run from
 // one runtime loop over the six transform stages of a pair, so the kernel's
 // code stays small enough for the instruction caches.
 //
@@ -77,6 +78,8 @@ __device__ __forceinline__ void put(float2& z, float f)
     else z.x = f;
 }
 
+// Pixel x goes to register bitrev(x): the row transform takes bit-reversed
+// input.
 template <int W, bool B, typename PixT, bool VEC>
 __device__ __forceinline__ void load_row(const PixT* ptr, float2 (&v)[W])
 {
@@ -85,10 +88,10 @@ __device__ __forceinline__ void load_row(const PixT* ptr, float2 (&v)[W])
 #pragma unroll
         for (int k = 0; k < W / 8; ++k) {
             const uint4 r = __ldg(q + k);
-            put<B>(v[8 * k + 0], u16_lo(r.x)); put<B>(v[8 * k + 1], u16_hi(r.x));
-            put<B>(v[8 * k + 2], u16_lo(r.y)); put<B>(v[8 * k + 3], u16_hi(r.y));
-            put<B>(v[8 * k + 4], u16_lo(r.z)); put<B>(v[8 * k + 5], u16_hi(r.z));
-            put<B>(v[8 * k + 6], u16_lo(r.w)); put<B>(v[8 * k + 7], u16_hi(r.w));
+            put<B>(v[bitrev<W>(8 * k + 0)], u16_lo(r.x)); put<B>(v[bitrev<W>(8 * k + 1)], u16_hi(r.x));
+            put<B>(v[bitrev<W>(8 * k + 2)], u16_lo(r.y)); put<B>(v[bitrev<W>(8 * k + 3)], u16_hi(r.y));
+            put<B>(v[bitrev<W>(8 * k + 4)], u16_lo(r.z)); put<B>(v[bitrev<W>(8 * k + 5)], u16_hi(r.z));
+            put<B>(v[bitrev<W>(8 * k + 6)], u16_lo(r.w)); put<B>(v[bitrev<W>(8 * k + 7)], u16_hi(r.w));
         }
     } else if (VEC && sizeof(PixT) == 1) {
         const uint4* q = reinterpret_cast<const uint4*>(ptr);
@@ -98,10 +101,10 @@ __device__ __forceinline__ void load_row(const PixT* ptr, float2 (&v)[W])
             const uint32_t w4[4] = { r.x, r.y, r.z, r.w };
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                put<B>(v[16 * k + 4 * j + 0], u8_k<0>(w4[j]));
-                put<B>(v[16 * k + 4 * j + 1], u8_k<1>(w4[j]));
-                put<B>(v[16 * k + 4 * j + 2], u8_k<2>(w4[j]));
-                put<B>(v[16 * k + 4 * j + 3], u8_k<3>(w4[j]));
+                put<B>(v[bitrev<W>(16 * k + 4 * j + 0)], u8_k<0>(w4[j]));
+                put<B>(v[bitrev<W>(16 * k + 4 * j + 1)], u8_k<1>(w4[j]));
+                put<B>(v[bitrev<W>(16 * k + 4 * j + 2)], u8_k<2>(w4[j]));
+                put<B>(v[bitrev<W>(16 * k + 4 * j + 3)], u8_k<3>(w4[j]));
             }
         }
     } else if (VEC && sizeof(PixT) == 4) {
@@ -109,24 +112,26 @@ __device__ __forceinline__ void load_row(const PixT* ptr, float2 (&v)[W])
 #pragma unroll
         for (int k = 0; k < W / 4; ++k) {
             const float4 r = __ldg(q + k);
-            put<B>(v[4 * k + 0], r.x); put<B>(v[4 * k + 1], r.y);
-            put<B>(v[4 * k + 2], r.z); put<B>(v[4 * k + 3], r.w);
+            put<B>(v[bitrev<W>(4 * k + 0)], r.x); put<B>(v[bitrev<W>(4 * k + 1)], r.y);
+            put<B>(v[bitrev<W>(4 * k + 2)], r.z); put<B>(v[bitrev<W>(4 * k + 3)], r.w);
         }
     } else {
 #pragma unroll
-        for (int x = 0; x < W; ++x) put<B>(v[x], (float)__ldg(ptr + x));
+        for (int x = 0; x < W; ++x) put<B>(v[bitrev<W>(x)], (float)__ldg(ptr + x));
     }
 }
 
-__device__ __forceinline__ void window_origin(const PivParams& p, int64_t w, int& bx, int& by)
+// Bottom-left corner of window w.  Window indices fit in 32 bits (plans
+// hold at most 2^31 - 1 windows), so the grid position is a 32-bit division.
+__device__ __forceinline__ void window_origin(const PivParams& p, int w, int& bx, int& by)
 {
     if (p.win_xy != nullptr) {
         bx = p.win_xy[2 * w];
         by = p.win_xy[2 * w + 1];
     } else {
-        const int64_t gy = w / p.gnx, gx = w - gy * p.gnx;
-        bx = p.gx0 + (int)gx * p.gdx;
-        by = p.gy0 + (int)gy * p.gdy;
+        const int gy = (int)((unsigned)w / (unsigned)p.gnx);
+        bx = p.gx0 + (w - gy * p.gnx) * p.gdx;
+        by = p.gy0 + gy * p.gdy;
     }
 }
 
@@ -149,12 +154,19 @@ __device__ __forceinline__ float group_max(float x)
 // accesses by the W lanes of a group hit distinct banks.
 template <int W>
 __device__ __forceinline__ int tix(int r, int c) { return r * (W + 1) + c; }
+// Hermitian half of a W x W spectrum: columns 0 .. W/2, rows padded.
+template <int W>
+__device__ __forceinline__ int hix(int r, int c) { return r * (W / 2 + 1) + c; }
+
+// shared memory per lane group: transpose tile + half spectrum
+template <int W>
+__host__ __device__ constexpr int group_smem_float2() { return W * (W + 1) + W * (W / 2 + 1); }
 
 // Transform stages of a pair, run by one runtime loop around one FFT body.
 enum { kStLoad0 = 0, kStCol0 = 1, kStLoad1 = 2, kStCol1 = 3, kStInvA = 4, kStInvB = 5 };
 
 template <int W, int MODE, bool LIMIT, typename PixT, bool PLANES, bool VEC>
-__global__ void __launch_bounds__(32 * kWarps, (W == 32 ? 3 : 4))
+__global__ void __launch_bounds__(32 * kWarps, 4)
 piv_fp32_kernel(const PivParams p)
 {
     constexpr int NG = 32 / W;          // lane groups per warp
@@ -166,30 +178,30 @@ piv_fp32_kernel(const PivParams p)
     constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
 
-    __shared__ float2 smem[kWarps][NG][W * (W + 1)];
+    extern __shared__ float2 dyn_smem[];
 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int grp = lane / W;
     const int gl = lane % W;
-    const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
-    const int64_t first = task * 2 * NG;
-    if (first >= p.n_win) return;   // warp-uniform
-    float2* S = smem[warp][grp];
+    const int task = blockIdx.x * kWarps + warp;
+    const int first = task * 2 * NG;
+    if (first >= (int)p.n_win) return;   // warp-uniform
+    float2* S = dyn_smem + (warp * NG + grp) * group_smem_float2<W>();   // transpose tile
+    float2* H = S + W * (W + 1);                                          // first product, half
 
     const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
     const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
     const size_t pitch = p.pitch / sizeof(PixT);
 
     float2 v[W];      // the transform being worked on
-    float2 Q[W];      // conj(P1) + i conj(P2), lane = kx, register i <-> ky = bitrev(i)
     float en0 = 0.f, en1 = 0.f, ped0 = 0.f, ped1 = 0.f;
 
 #pragma unroll 1
     for (int st = 0; st < 6; ++st) {
         const int h = (st >= kStLoad1 && st <= kStCol1) ? 1 : 0;
-        const int64_t w = first + h * NG + grp;
-        const bool valid = w < p.n_win;
+        const int w = first + h * NG + grp;
+        const bool valid = w < (int)p.n_win;
         // ---------------- before the transform
         if (st == kStLoad0 || st == kStLoad1) {
             // extract + widen: lane = row y, registers = x
@@ -199,6 +211,17 @@ piv_fp32_kernel(const PivParams p)
                 const size_t off = (size_t)(by + gl) * pitch + bx;
                 load_row<W, false, PixT, VEC>(fa + off, v);
                 load_row<W, true, PixT, VEC>(fb + off, v);
+                if (PLANES) {   // exact pedestal for the per-window API (double input)
+                    double sa = 0.0, sb = 0.0;
+#pragma unroll 4
+                    for (int x = 0; x < W; ++x) {
+                        sa += (double)fa[off + x];
+                        sb += (double)fb[off + x];
+                    }
+                    sa = group_sum<W, double>(sa);
+                    sb = group_sum<W, double>(sb);
+                    if (gl == 0) p.peds[w] = (MODE == kModeComplex) ? sa * sb : 0.0;
+                }
             } else {
 #pragma unroll
                 for (int x = 0; x < W; ++x) v[x] = make_float2(0.f, 0.f);
@@ -208,60 +231,41 @@ piv_fp32_kernel(const PivParams p)
             for (int x = 0; x < W; ++x) e = fmaf(v[x].x, v[x].x, fmaf(v[x].y, v[x].y, e));
             e = group_sum<W, float>(e);
             if (h == 0) en0 = e; else en1 = e;
-            if (PLANES && valid) {   // exact pedestal for the per-window API (double input)
-                double sa = 0.0, sb = 0.0;
-                const double* da = reinterpret_cast<const double*>(fa);
-                const double* db = reinterpret_cast<const double*>(fb);
-                int bx, by;
-                window_origin(p, w, bx, by);
-#pragma unroll 4
-                for (int x = 0; x < W; ++x) {
-                    sa += da[(size_t)(by + gl) * pitch + bx + x];
-                    sb += db[(size_t)(by + gl) * pitch + bx + x];
-                }
-                sa = group_sum<W, double>(sa);
-                sb = group_sum<W, double>(sb);
-                if (gl == 0) p.peds[w] = (MODE == kModeComplex) ? sa * sb : 0.0;
-            }
         } else if (st == kStCol0 || st == kStCol1) {
-            // v: lane = y, register i <-> kx = bitrev(i).  Transpose to
-            // lane = kx, registers = y.  REAL mode: column kx = 0 of Z is
-            // zeroed here (register 0), so lane 0's spectrum is zero.
+            // v: lane = y, register kx.  Transpose to lane = kx, register
+            // bitrev(y).  REAL mode: column kx = 0 of Z is zeroed here, so
+            // lane 0's spectrum is zero.
 #pragma unroll
-            for (int i = 0; i < W; ++i) {
-                const float2 z = (MODE == kModeReal && i == 0) ? make_float2(0.f, 0.f) : v[i];
-                S[tix<W>(bitrev<W>(i), gl)] = z;
+            for (int kx = 0; kx < W; ++kx) {
+                const float2 z = (MODE == kModeReal && kx == 0) ? make_float2(0.f, 0.f) : v[kx];
+                S[tix<W>(kx, gl)] = z;
             }
             __syncwarp();
 #pragma unroll
-            for (int y = 0; y < W; ++y) v[y] = S[tix<W>(gl, y)];
+            for (int y = 0; y < W; ++y) v[bitrev<W>(y)] = S[tix<W>(gl, y)];
             __syncwarp();
         } else if (st == kStInvA) {
-            // Q: lane = kx, register i <-> ky = bitrev(i).  To lane = ky,
-            // registers = kx.
+            // S holds Q at [ky][kx] (written by the second unpack).  To
+            // lane = ky, register bitrev(kx).
 #pragma unroll
-            for (int i = 0; i < W; ++i) S[tix<W>(bitrev<W>(i), gl)] = Q[i];
-            __syncwarp();
-#pragma unroll
-            for (int x = 0; x < W; ++x) v[x] = S[tix<W>(gl, x)];
+            for (int x = 0; x < W; ++x) v[bitrev<W>(x)] = S[tix<W>(gl, x)];
             __syncwarp();
         } else {   // kStInvB
-            // v: lane = ky, register i <-> x = bitrev(i).  To lane = x,
-            // registers = ky.
+            // v: lane = ky, register x.  To lane = x, register bitrev(ky).
 #pragma unroll
-            for (int i = 0; i < W; ++i) S[tix<W>(bitrev<W>(i), gl)] = v[i];
+            for (int x = 0; x < W; ++x) S[tix<W>(x, gl)] = v[x];
             __syncwarp();
 #pragma unroll
-            for (int y = 0; y < W; ++y) v[y] = S[tix<W>(gl, y)];
+            for (int y = 0; y < W; ++y) v[bitrev<W>(y)] = S[tix<W>(gl, y)];
             __syncwarp();
         }
 
-        fft_dif<W, false>(v);
+        fft_dit_fma<W, false>(v);
 
         // ---------------- after the transform
         if (st == kStCol0 || st == kStCol1) {
-            // v: lane = kx, register i <-> ky = bitrev(i).  DC bin = (sum a,
-            // sum b) on lane 0, register 0.
+            // v: lane = kx, register ky.  DC bin = (sum a, sum b) on lane 0,
+            // register 0.
             const float2 dc = make_float2(__shfl_sync(0xffffffffu, v[0].x, 0, W),
                                           __shfl_sync(0xffffffffu, v[0].y, 0, W));
             const float pd = (MODE == kModeComplex) ? 4.f * dc.x * dc.y : 0.f;
@@ -269,26 +273,37 @@ piv_fp32_kernel(const PivParams p)
             if (MODE == kModeComplex && gl == 0) v[0] = make_float2(0.f, 0.f);
             if (MODE == kModeReal) {   // rows ky = 0 and ky = W/2
                 v[0] = make_float2(0.f, 0.f);
-                v[1] = make_float2(0.f, 0.f);
+                v[W / 2] = make_float2(0.f, 0.f);
             }
             const int pl = (W - gl) & (W - 1);
+            // first window: its product goes to the half spectrum H (lanes
+            // kx <= W/2); second window: lanes kx > W/2 take the first product
+            // from the mirror (-ky, W - kx) of H, conjugated, and Q goes to S
+            const bool mirror = gl > W / 2;
+            const int hc = mirror ? W - gl : gl;
+            const float sg = mirror ? -1.f : 1.f;
+            const bool store_h = (h == 0) && !mirror;
 #pragma unroll
-            for (int i = 0; i < W; ++i) {
-                const int ky = bitrev<W>(i);
-                const int mi = bitrev<W>((W - ky) & (W - 1));
-                const float2 z = v[i];
-                const float zmx = __shfl_sync(0xffffffffu, v[mi].x, pl, W);
-                const float zmy = __shfl_sync(0xffffffffu, v[mi].y, pl, W);
+            for (int ky = 0; ky < W; ++ky) {
+                const int mky = (W - ky) & (W - 1);
+                const float2 z = v[ky];
+                const float zmx = __shfl_sync(0xffffffffu, v[mky].x, pl, W);
+                const float zmy = __shfl_sync(0xffffffffu, v[mky].y, pl, W);
                 // 4 conj(P) = ( 2 Im(Z Zm), |Z|^2 - |Zm|^2 )
                 const float im2 = 2.f * fmaf(z.x, zmy, z.y * zmx);
                 const float d = fmaf(z.x, z.x, fmaf(z.y, z.y, -fmaf(zmx, zmx, zmy * zmy)));
-                if (h == 0) Q[i] = make_float2(im2, d);
-                else Q[i] = make_float2(Q[i].x - d, Q[i].y + im2);
+                if (store_h) H[hix<W>(ky, gl)] = make_float2(im2, d);
+                if (h == 1) {
+                    // Q = conj(4 P1) + i conj(4 P2), stored at [ky][kx]
+                    const float2 c1 = H[hix<W>(mirror ? mky : ky, hc)];
+                    S[tix<W>(ky, gl)] = make_float2(c1.x - d, fmaf(sg, c1.y, im2));
+                }
             }
+            __syncwarp();
         }
     }
-    // v: lane = x, register i <-> y = bitrev(i); v.x = plane of the first
-    // window of the pair, v.y of the second (4x scaled, pedestal removed).
+    // v: lane = x, register y; v.x = plane of the first window of the pair,
+    // v.y of the second (4x scaled, pedestal removed).
 
     const float dlt = p.kappa * 5.9604645e-8f * 2.f * (float)N * (en0 + en1);
     const int xs = (gl + W / 2) & (W - 1);          // swapped column of this lane
@@ -296,20 +311,21 @@ piv_fp32_kernel(const PivParams p)
 
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
-        const int64_t w = first + h * NG + grp;
-        const bool valid = w < p.n_win;
-        float val[W];                                // val[i] <-> y = bitrev(i)
+        const int w = first + h * NG + grp;
+        const bool valid = w < (int)p.n_win;
+        if (h == 1) {                                // the second plane into .x
 #pragma unroll
-        for (int i = 0; i < W; ++i) val[i] = h ? v[i].y : v[i].x;
+            for (int i = 0; i < W; ++i) v[i].x = v[i].y;
+        }
 
         // plane rows y into shared memory (row-major, padded) for the fit
 #pragma unroll
-        for (int i = 0; i < W; ++i) S[tix<W>(bitrev<W>(i), gl)] = make_float2(val[i], 0.f);
+        for (int y = 0; y < W; ++y) S[tix<W>(y, gl)].x = v[y].x;
         if (PLANES && valid) {
 #pragma unroll
-            for (int i = 0; i < W; ++i) {
-                const int ys = (bitrev<W>(i) + W / 2) & (W - 1);
-                p.planes[(size_t)w * N + ys * W + xs] = 0.25f * val[i];
+            for (int y = 0; y < W; ++y) {
+                const int ys = (y + W / 2) & (W - 1);
+                p.planes[(size_t)w * N + ys * W + xs] = 0.25f * v[y].x;
             }
         }
 
@@ -319,9 +335,9 @@ piv_fp32_kernel(const PivParams p)
 #pragma unroll
         for (int ys = SY0; ys < SY1; ++ys) {
             const int y = (ys + W / 2) & (W - 1);
-            const float c = val[bitrev<W>(y)];
-            const float up = val[bitrev<W>((y + W - 1) & (W - 1))];
-            const float dn = val[bitrev<W>((y + 1) & (W - 1))];
+            const float c = v[y].x;
+            const float up = v[(y + W - 1) & (W - 1)].x;
+            const float dn = v[(y + 1) & (W - 1)].x;
             const float lf = __shfl_sync(0xffffffffu, c, (gl + W - 1) & (W - 1), W);
             const float rt = __shfl_sync(0xffffffffu, c, (gl + 1) & (W - 1), W);
             const float dd = fmaxf(fmaxf(up, dn), fmaxf(lf, rt)) - c;
@@ -436,10 +452,17 @@ cudaError_t launch_t(const PivParams& p, cudaStream_t s)
                      ((uintptr_t)p.fb % 16 == 0) && (p.pitch % 16 == 0) &&
                      (((size_t)p.gx0 * px) % 16 == 0) && (((size_t)p.gdx * px) % 16 == 0) &&
                      ((W * px) % 16 == 0);
-    if (vec)
-        piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, true><<<(unsigned)blocks, 32 * kWarps, 0, s>>>(p);
-    else
-        piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, false><<<(unsigned)blocks, 32 * kWarps, 0, s>>>(p);
+    const size_t smem = sizeof(float2) * kWarps * NG * group_smem_float2<W>();
+    auto kern = vec ? piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, true>
+                    : piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, false>;
+    static bool attr_done[2] = { false, false };   // per instantiation and load path
+    if (!attr_done[vec]) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_done[vec] = true;
+    }
+    kern<<<(unsigned)blocks, 32 * kWarps, smem, s>>>(p);
     return cudaGetLastError();
 }
 
