@@ -151,6 +151,20 @@ int opiv_process_pair_device_noalloc(const void* d_frame_a, const void* d_frame_
 int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int64_t n, int mode,
                                int exact, double* out_planes, int device);
 
+/* ---- image ingest and vector output (host) ------------------------------- */
+/* The reference's loaders (loaders/pnm_image_loader.cpp:199-226, PNM P5/P6,
+ * 8- or 16-bit big-endian samples; loaders/tiff_image_loader.cpp:190-226,
+ * TIFF through libtiff) deliver 8/16-bit grey samples (RGB -> grey with
+ * (218 r + 732 g + 74 b) >> 10, pixel_types.h:390-400).  These read PNM and
+ * baseline uncompressed TIFF (8/16-bit, 1 or 3 samples, first image) without
+ * external libraries.  dtype: OPIV_U8 for 8-bit files, OPIV_U16 for 16-bit. */
+int opiv_image_info(const char* path, uint32_t* width, uint32_t* height, int* dtype);
+int opiv_image_load(const char* path, void* out, size_t pitch_bytes, uint32_t width,
+                    uint32_t height, int dtype);
+/* One "x, y, u, v, sn" line per window, as main.cpp:312-313 prints them
+ * (6 significant digits); path NULL or "-" writes to stdout. */
+int opiv_vectors_write(const char* path, const opiv_vector* vectors, int64_t n);
+
 /* ---- host helpers of the same path (no GPU) ------------------------------ */
 /* core::find_peaks(im, num_peaks, radius): image_utils.impl.h:42-74.  Writes
  * up to num_peaks centres (x, y) and values, highest first; returns count. */

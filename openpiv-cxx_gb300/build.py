@@ -79,7 +79,30 @@ def build(verbose: bool = False) -> str:
         if rc != 0:
             sys.stderr.write(out)
             raise RuntimeError("link failed")
+    build_examples()
     return LIB
+
+
+def build_examples() -> list[str]:
+    """The C++ example programs (examples/*.cpp) against the library."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("a C++ compiler is required to build the examples")
+    exes = []
+    for src in sorted(glob.glob(os.path.join(HERE, "examples", "*.cpp"))):
+        exe = os.path.join(HERE, "lib", os.path.splitext(os.path.basename(src))[0])
+        deps = [src, LIB, os.path.join(HERE, "cpp", "openpiv_gb300.hpp"),
+                os.path.join(INCLUDE, "openpiv_gb300.h")]
+        if not os.path.exists(exe) or any(os.path.getmtime(d) > os.path.getmtime(exe) for d in deps):
+            args = [cxx, "-std=c++17", "-O2", "-Wall", "-I", INCLUDE, "-I", os.path.join(HERE, "cpp"),
+                    src, "-L", os.path.dirname(LIB), "-lopenpiv_gb300",
+                    "-Wl,-rpath,$ORIGIN", "-o", exe]
+            _, rc, out = _compile(args)
+            if rc != 0:
+                sys.stderr.write(out)
+                raise RuntimeError(f"example build failed: {src}")
+        exes.append(exe)
+    return exes
 
 
 if __name__ == "__main__":

@@ -46,6 +46,7 @@ SYMBOLS = [
     "opiv_process_pair_device", "opiv_plan_exact_count", "opiv_plan_set_timing",
     "opiv_plan_last_timing", "opiv_cross_correlate_batch",
     "opiv_find_peaks", "opiv_fit_simple_gaussian", "opiv_process_pair_device_noalloc",
+    "opiv_image_info", "opiv_image_load", "opiv_vectors_write",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -104,6 +105,11 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_process_pair_device_noalloc.argtypes = [
         C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32, C.c_int, C.c_uint32,
         C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.opiv_image_info.argtypes = [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                  C.POINTER(C.c_int)]
+    L.opiv_image_load.argtypes = [C.c_char_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32,
+                                  C.c_int]
+    L.opiv_vectors_write.argtypes = [C.c_char_p, C.c_void_p, C.c_int64]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -265,3 +271,21 @@ def fit_simple_gaussian(plane: np.ndarray, px: int, py: int) -> np.ndarray:
     _check(load().opiv_fit_simple_gaussian(plane.ctypes.data_as(_dp), plane.shape[1],
                                            plane.shape[0], px, py, out.ctypes.data_as(_dp)))
     return out
+
+
+# ---- image ingest and vector output ---------------------------------------
+def load_image(path: str) -> np.ndarray:
+    """PNM (P5/P6) or uncompressed TIFF -> (h, w) uint8 or uint16 grey samples."""
+    L = load()
+    w, h, dt = C.c_uint32(), C.c_uint32(), C.c_int()
+    _check(L.opiv_image_info(path.encode(), C.byref(w), C.byref(h), C.byref(dt)))
+    out = np.zeros((h.value, w.value), np.uint16 if dt.value == U16 else np.uint8)
+    _check(L.opiv_image_load(path.encode(), out.ctypes.data, out.strides[0], w.value, h.value,
+                             dt.value))
+    return out
+
+
+def write_vectors(path: str, vectors: np.ndarray) -> None:
+    """The reference app's text output: one "x, y, u, v, sn" line per window."""
+    v = np.ascontiguousarray(vectors, np.float32)
+    _check(load().opiv_vectors_write(path.encode(), v.ctypes.data, v.shape[0]))
