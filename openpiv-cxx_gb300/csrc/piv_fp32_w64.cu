@@ -1,0 +1,378 @@
+// piv_fp32_w64.cu -- fused FP32 PIV kernel for 64 x 64 windows (sm_103a).
+//
+// A 64-point row does not fit one lane's registers next to everything else,
+// so this kernel keeps the pair's spectra in shared memory: one CTA of 256
+// threads per pair of windows, two padded 64 x 65 float2 tiles.  The steps
+// and the formulas are those of the 16/32 kernel (piv_fp32.cuh):
+//   z = a + i b; 2-D FFT (rows, then columns) as radix-4 decimation-in-
+//   frequency passes over the tile (64 = 4^3; outputs in base-4 digit-
+//   reversed order, absorbed in the indexing);
+//   4 conj(P) = (2 Im(Z Zm), |Z|^2 - |Zm|^2) with Zm = Z[-k] (P = B conj A,
+//   fft.h:188-227), REAL mode's zeroed spectrum row 0, row W/2, column 0
+//   (fft.h:166-183), DC product dropped and the pedestal added back;
+//   Q = conj(4 P1) + i conj(4 P2), one forward 2-D FFT -> both planes;
+//   find_peaks(plane, 2, 1) (image_utils.impl.h:42-74) as a block scan and
+//   reduction; fit_simple_gaussian (impl:77-101); vector of main.cpp:220-236;
+//   the same certification and hand-off to the exact kernel.
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fft_reg.cuh"
+#include "piv_kernels.h"
+
+namespace opiv {
+namespace w64 {
+
+constexpr int W = 64;
+constexpr int N = W * W;
+constexpr int LD = W + 1;            // padded row stride (float2)
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr float kFitTol = 3e-5f;
+constexpr float kSnTol = 3e-6f;
+#define kNegInf64 (-__int_as_float(0x7f800000))
+
+// base-4 digit reversal of a 6-bit index (an involution)
+__device__ __forceinline__ int dr(int v) { return ((v & 3) << 4) | (v & 12) | (v >> 4); }
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 w)
+{
+    return make_float2(fmaf(a.x, w.x, -a.y * w.y), fmaf(a.x, w.y, a.y * w.x));
+}
+
+// Forward radix-4 DIF over all 64 lines of tile T; rows when `rows`, else
+// columns.  tw[k] = exp(-2 pi i k / 64).  Each line ends in base-4 digit-
+// reversed order.
+__device__ void dif4_lines(float2* T, bool rows, const float2* tw)
+{
+    const int es = rows ? 1 : LD, ls = rows ? LD : 1;
+    for (int q = 16; q >= 1; q >>= 2) {
+        for (int k = threadIdx.x; k < 64 * 16; k += kThreads) {
+            // rows: neighbouring threads walk along a line; columns: across lines
+            const int line = rows ? (k >> 4) : (k & 63);
+            const int b = rows ? (k & 15) : (k >> 6);
+            const int j = b % q;
+            const int base = (b / q) * 4 * q + j;
+            float2* x = T + line * ls;
+            const float2 a = x[base * es], bb = x[(base + q) * es];
+            const float2 c = x[(base + 2 * q) * es], d = x[(base + 3 * q) * es];
+            const float2 t0 = make_float2(a.x + c.x, a.y + c.y), t1 = make_float2(a.x - c.x, a.y - c.y);
+            const float2 t2 = make_float2(bb.x + d.x, bb.y + d.y), t3 = make_float2(bb.x - d.x, bb.y - d.y);
+            // length-4 DFT, forward: y1 = t1 - i t3, y3 = t1 + i t3
+            const float2 y0 = make_float2(t0.x + t2.x, t0.y + t2.y);
+            const float2 y2 = make_float2(t0.x - t2.x, t0.y - t2.y);
+            const float2 y1 = make_float2(t1.x + t3.y, t1.y - t3.x);
+            const float2 y3 = make_float2(t1.x - t3.y, t1.y + t3.x);
+            const int s = 16 / q;   // W_{4q}^{j m} = tw[j m 64 / (4q)]
+            x[base * es] = y0;
+            x[(base + q) * es] = cmul(y1, tw[(j * s) & 63]);
+            x[(base + 2 * q) * es] = cmul(y2, tw[(2 * j * s) & 63]);
+            x[(base + 3 * q) * es] = cmul(y3, tw[(3 * j * s) & 63]);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void fft2d(float2* T, const float2* tw)
+{
+    dif4_lines(T, true, tw);
+    dif4_lines(T, false, tw);
+}
+
+// position in a transformed tile of spectrum bin (ky, kx) / plane (y, x)
+__device__ __forceinline__ int at(int r, int c) { return dr(r) * LD + dr(c); }
+
+__device__ __forceinline__ void window_origin(const PivParams& p, int w, int& bx, int& by)
+{
+    if (p.win_xy != nullptr) {
+        bx = p.win_xy[2 * w];
+        by = p.win_xy[2 * w + 1];
+    } else {
+        const int gy = (int)((unsigned)w / (unsigned)p.gnx);
+        bx = p.gx0 + (w - gy * p.gnx) * p.gdx;
+        by = p.gy0 + gy * p.gdy;
+    }
+}
+
+__device__ __forceinline__ float block_sum(float v, float* red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float s = 0.f;
+    for (int i = 0; i < kWarps; ++i) s += red[i];
+    __syncthreads();
+    return s;
+}
+
+template <int MODE, bool LIMIT, typename PixT, bool PLANES>
+__global__ void __launch_bounds__(kThreads, 3)
+piv_w64_kernel(const PivParams p)
+{
+    constexpr int D0 = LIMIT ? W / 4 : 0;
+    constexpr int VW = LIMIT ? W / 2 : W;
+    constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
+    constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
+
+    extern __shared__ float2 sm[];
+    float2* T1 = sm;                  // first window, then Q, then both planes
+    float2* T2 = sm + W * LD;         // second window
+    __shared__ float2 tw[64];
+    __shared__ float red[kWarps * 4];
+    __shared__ float rv0[kWarps], rv1[kWarps], ru[kWarps];
+    __shared__ int rk[kWarps];
+    __shared__ float sped[2];
+
+    const int t = threadIdx.x;
+    const int w0 = 2 * blockIdx.x;
+    if (w0 >= (int)p.n_win) return;
+    const int w1 = w0 + 1;
+    const bool valid1 = w1 < (int)p.n_win;
+    if (t < 64) tw[t] = make_float2(c_tw.re[t], c_tw.im[t]);
+
+    const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
+    const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
+    const size_t pitch = p.pitch / sizeof(PixT);
+
+    // ---- extract, widen, energies (and the exact pedestal for the batch API)
+    int bx0, by0, bx1 = 0, by1 = 0;
+    window_origin(p, w0, bx0, by0);
+    if (valid1) window_origin(p, w1, bx1, by1);
+    float e0 = 0.f, e1 = 0.f;
+    double sa0 = 0.0, sb0 = 0.0, sa1 = 0.0, sb1 = 0.0;
+    for (int i = t; i < N; i += kThreads) {
+        const int y = i >> 6, x = i & 63;
+        const double a0 = (double)__ldg(fa + (size_t)(by0 + y) * pitch + bx0 + x);
+        const double b0 = (double)__ldg(fb + (size_t)(by0 + y) * pitch + bx0 + x);
+        double a1 = 0.0, b1 = 0.0;
+        if (valid1) {
+            a1 = (double)__ldg(fa + (size_t)(by1 + y) * pitch + bx1 + x);
+            b1 = (double)__ldg(fb + (size_t)(by1 + y) * pitch + bx1 + x);
+        }
+        const float2 z0 = make_float2((float)a0, (float)b0), z1 = make_float2((float)a1, (float)b1);
+        T1[y * LD + x] = z0;
+        T2[y * LD + x] = z1;
+        e0 = fmaf(z0.x, z0.x, fmaf(z0.y, z0.y, e0));
+        e1 = fmaf(z1.x, z1.x, fmaf(z1.y, z1.y, e1));
+        if (PLANES) { sa0 += a0; sb0 += b0; sa1 += a1; sb1 += b1; }
+    }
+    e0 = block_sum(e0, red);
+    e1 = block_sum(e1, red);
+    if (PLANES) {
+        const double s[4] = { sa0, sb0, sa1, sb1 };
+        double tot[4];
+        for (int c = 0; c < 4; ++c) {
+            double v = s[c];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            __syncthreads();
+            if ((t & 31) == 0) reinterpret_cast<double*>(red)[t >> 5] = v;
+            __syncthreads();
+            double acc = 0.0;
+            for (int i = 0; i < kWarps; ++i) acc += reinterpret_cast<double*>(red)[i];
+            tot[c] = acc;
+            __syncthreads();
+        }
+        if (t == 0) {
+            p.peds[w0] = (MODE == kModeComplex) ? tot[0] * tot[1] : 0.0;
+            if (valid1) p.peds[w1] = (MODE == kModeComplex) ? tot[2] * tot[3] : 0.0;
+        }
+    }
+    __syncthreads();
+
+    // ---- forward transforms
+    fft2d(T1, tw);
+    fft2d(T2, tw);
+    if (t == 0) {   // DC bins: (sum a, sum b) of each window
+        const float2 d0 = T1[0], d1 = T2[0];
+        sped[0] = (MODE == kModeComplex) ? 4.f * d0.x * d0.y : 0.f;
+        sped[1] = (MODE == kModeComplex) ? 4.f * d1.x * d1.y : 0.f;
+    }
+    __syncthreads();
+    // zero the DC bin (COMPLEX) or the reference's unpacked-out set (REAL)
+    for (int i = t; i < N; i += kThreads) {
+        const int ky = i >> 6, kx = i & 63;
+        const bool zero = (MODE == kModeReal) ? (ky == 0 || ky == W / 2 || kx == 0)
+                                              : (ky == 0 && kx == 0);
+        if (zero) {
+            T1[at(ky, kx)] = make_float2(0.f, 0.f);
+            T2[at(ky, kx)] = make_float2(0.f, 0.f);
+        }
+    }
+    __syncthreads();
+
+    // ---- products, packed: Q[ky][kx] = conj(4 P1) + i conj(4 P2), written
+    // in natural order (the next transform is a forward DIF again)
+    float2 q[N / kThreads];
+#pragma unroll
+    for (int n = 0; n < N / kThreads; ++n) {
+        const int i = t + n * kThreads;
+        const int ky = i >> 6, kx = i & 63;
+        const int mky = (W - ky) & (W - 1), mkx = (W - kx) & (W - 1);
+        const float2 z1 = T1[at(ky, kx)], m1 = T1[at(mky, mkx)];
+        const float2 z2 = T2[at(ky, kx)], m2 = T2[at(mky, mkx)];
+        const float im1 = 2.f * fmaf(z1.x, m1.y, z1.y * m1.x);
+        const float d1 = fmaf(z1.x, z1.x, fmaf(z1.y, z1.y, -fmaf(m1.x, m1.x, m1.y * m1.y)));
+        const float im2 = 2.f * fmaf(z2.x, m2.y, z2.y * m2.x);
+        const float d2 = fmaf(z2.x, z2.x, fmaf(z2.y, z2.y, -fmaf(m2.x, m2.x, m2.y * m2.y)));
+        q[n] = make_float2(im1 - d2, d1 + im2);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < N / kThreads; ++n) {
+        const int i = t + n * kThreads;
+        T1[(i >> 6) * LD + (i & 63)] = q[n];
+    }
+    __syncthreads();
+    fft2d(T1, tw);   // T1[at(y, x)] = plane1(y, x) + i plane2(y, x), 4x scaled
+
+    const float dlt = p.kappa * 5.9604645e-8f * 2.f * (float)N * (e0 + e1);
+    const int lane = t & 31, wp = t >> 5;
+
+    for (int h = 0; h < 2; ++h) {
+        const int w = h ? w1 : w0;
+        const bool valid = h ? valid1 : true;
+        const float ped = sped[h];
+        auto val = [&](int ys, int xs) -> float {   // swapped-plane value
+            const float2 v = T1[at((ys + W / 2) & (W - 1), (xs + W / 2) & (W - 1))];
+            return h ? v.y : v.x;
+        };
+        if (PLANES && valid)
+            for (int i = t; i < N; i += kThreads)
+                p.planes[(size_t)w * N + i] = 0.25f * val(i >> 6, i & 63);
+
+        // ---- find_peaks: thread = (column, 16-row block), then block reduce
+        const int xs = t & 63, yb = (t >> 6) * 16;
+        const bool col_ok = xs >= SX0 && xs < SX1;
+        float t0 = kNegInf64, t1 = kNegInf64, umax = kNegInf64;
+        int key = 0x7fffffff;
+        for (int ys = yb; ys < yb + 16; ++ys) {
+            if (!(col_ok && ys >= SY0 && ys < SY1)) continue;
+            const float c = val(ys, xs);
+            const float m = fmaxf(fmaxf(val(ys - 1, xs), val(ys + 1, xs)),
+                                  fmaxf(val(ys, xs - 1), val(ys, xs + 1)));
+            const float dd = m - c;
+            if (fabsf(dd) <= dlt) umax = fmaxf(umax, c);
+            if (dd < 0.f) {
+                if (c > t0) { t1 = t0; t0 = c; key = ys * W + xs; }
+                else t1 = fmaxf(t1, c);
+            }
+        }
+        // warp reduction (ties to the lowest row-major index)
+        for (int o = 16; o > 0; o >>= 1) {
+            const float o0 = __shfl_xor_sync(0xffffffffu, t0, o);
+            const float o1 = __shfl_xor_sync(0xffffffffu, t1, o);
+            const int ok = __shfl_xor_sync(0xffffffffu, key, o);
+            const bool take = (o0 > t0) || (o0 == t0 && ok < key);
+            const float n1 = take ? fmaxf(t0, o1) : fmaxf(t1, o0);
+            t0 = take ? o0 : t0;
+            key = take ? ok : key;
+            t1 = n1;
+            umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+        }
+        if (lane == 0) { rv0[wp] = t0; rv1[wp] = t1; rk[wp] = key; ru[wp] = umax; }
+        __syncthreads();
+        if (t == 0) {
+            float g0 = kNegInf64, g1 = kNegInf64, gu = kNegInf64;
+            int gk = 0x7fffffff;
+            for (int i = 0; i < kWarps; ++i) {
+                const bool take = (rv0[i] > g0) || (rv0[i] == g0 && rk[i] < gk);
+                const float n1 = take ? fmaxf(g0, rv1[i]) : fmaxf(g1, rv0[i]);
+                if (take) { g0 = rv0[i]; gk = rk[i]; }
+                g1 = n1;
+                gu = fmaxf(gu, ru[i]);
+            }
+            if (valid) {
+                opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
+                int32_t code = -1;
+                bool certain;
+                if (!(g1 > kNegInf64)) {
+                    certain = !(gu > kNegInf64);
+                } else {
+                    const int px = gk % W, py = gk / W;
+                    const float vc = val(py, px), vl = val(py, px - 1), vr = val(py, px + 1);
+                    const float vu = val(py - 1, px), vd = val(py + 1, px);
+                    const float C = vc + ped, L = vl + ped, R = vr + ped, U = vu + ped, D = vd + ped;
+                    const float nan = __int_as_float(0x7fffffff);
+                    const bool okx = L > 0.f && C > 0.f && R > 0.f;
+                    const bool oky = U > 0.f && C > 0.f && D > 0.f;
+                    const float denx = log1pf((vl - vc) / C) + log1pf((vr - vc) / C);
+                    const float deny = log1pf((vu - vc) / C) + log1pf((vd - vc) / C);
+                    const float fx = okx ? log1pf((vl - vr) / R) / (2.f * denx) : nan;
+                    const float fy = oky ? log1pf((vu - vd) / D) / (2.f * deny) : nan;
+                    const float mx = fminf(fminf(L, R), C), my = fminf(fminf(U, D), C);
+                    const float ex = okx ? (denx == 0.f ? 3.4e38f
+                                            : dlt * (1.f + 4.f * fabsf(fx)) / (mx * 2.f * fabsf(denx)))
+                                         : (mx < -dlt ? 0.f : 3.4e38f);
+                    const float ey = oky ? (deny == 0.f ? 3.4e38f
+                                            : dlt * (1.f + 4.f * fabsf(fy)) / (my * 2.f * fabsf(deny)))
+                                         : (my < -dlt ? 0.f : 3.4e38f);
+                    const float p0 = g0 + ped, p1 = g1 + ped;
+                    const float sn_err = 0.5f * dlt * (1.f / fabsf(p0) + 1.f / fabsf(p1));
+                    certain = (gu < g1 - 2.f * dlt) && (g0 - g1 > dlt) && (fabsf(p1) > dlt) &&
+                              (ex < kFitTol) && (ey < kFitTol) &&
+                              (p1 <= 0.f || sn_err < kSnTol * (1.f + p0 / p1));
+                    const int bx = h ? bx1 : bx0, by = h ? by1 : by0;
+                    out.x = (float)(bx + W / 2);
+                    out.y = (float)(p.img_h - (by + W / 2));
+                    out.u = (float)(W / 2 - px) - fx;
+                    out.v = (float)(W / 2 - py) - fy;
+                    out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
+                    code = gk;
+                }
+                p.out_vec[w] = out;
+                if (p.out_peak) p.out_peak[w] = code;
+                if (!certain && p.flag_list) {
+                    const unsigned int slot = atomicAdd(p.flag_count, 1u);
+                    p.flag_list[slot] = (int32_t)w;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int MODE, bool LIMIT, typename PixT, bool PLANES>
+cudaError_t launch_t(const PivParams& p, cudaStream_t s)
+{
+    const size_t smem = sizeof(float2) * 2 * W * LD;
+    static bool attr_done = false;
+    if (!attr_done) {
+        const cudaError_t e = cudaFuncSetAttribute(piv_w64_kernel<MODE, LIMIT, PixT, PLANES>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_done = true;
+    }
+    const int64_t blocks = (p.n_win + 1) / 2;
+    piv_w64_kernel<MODE, LIMIT, PixT, PLANES><<<(unsigned)blocks, kThreads, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <int MODE, bool LIMIT>
+cudaError_t launch_dt(const PivParams& p, int dtype, bool planes, cudaStream_t s)
+{
+    if (planes) return dtype == kF64 ? launch_t<MODE, LIMIT, double, true>(p, s) : cudaErrorInvalidValue;
+    switch (dtype) {
+    case kU8: return launch_t<MODE, LIMIT, uint8_t, false>(p, s);
+    case kU16: return launch_t<MODE, LIMIT, uint16_t, false>(p, s);
+    case kF32: return launch_t<MODE, LIMIT, float, false>(p, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace w64
+
+cudaError_t launch_piv_fp32_w64(const PivParams& p, int dtype, int mode, int limit, bool planes,
+                                cudaStream_t s)
+{
+    if (p.n_win <= 0) return cudaSuccess;
+    if (mode == kModeComplex)
+        return limit ? w64::launch_dt<kModeComplex, true>(p, dtype, planes, s)
+                     : w64::launch_dt<kModeComplex, false>(p, dtype, planes, s);
+    return limit ? w64::launch_dt<kModeReal, true>(p, dtype, planes, s)
+                 : w64::launch_dt<kModeReal, false>(p, dtype, planes, s);
+}
+
+}  // namespace opiv

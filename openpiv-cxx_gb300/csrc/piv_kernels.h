@@ -35,18 +35,22 @@ struct PivParams {
     const double2* tw_rev = nullptr;
 };
 
-// Fused FP32 kernel, one entry per window size (piv_fp32_w*.cu).  Frames
+// Fused FP32 kernels, one entry per window size (piv_fp32_w*.cu; 64 x 64
+// windows use the shared-memory kernel of piv_fp32_w64.cu).  Frames
 // (u8/u16/f32) without plane output; double windows (kF64) with planes.
 cudaError_t launch_piv_fp32_w16(const PivParams& p, int dtype, int mode, int limit, bool planes,
                                 cudaStream_t s);
 cudaError_t launch_piv_fp32_w32(const PivParams& p, int dtype, int mode, int limit, bool planes,
                                 cudaStream_t s);
-inline bool fp32_supports(int w) { return w == 16 || w == 32; }
+cudaError_t launch_piv_fp32_w64(const PivParams& p, int dtype, int mode, int limit, bool planes,
+                                cudaStream_t s);
+inline bool fp32_supports(int w) { return w == 16 || w == 32 || w == 64; }
 inline cudaError_t launch_piv_fp32(const PivParams& p, int w, int dtype, int mode, int limit,
                                    bool planes, cudaStream_t s)
 {
     if (w == 16) return launch_piv_fp32_w16(p, dtype, mode, limit, planes, s);
     if (w == 32) return launch_piv_fp32_w32(p, dtype, mode, limit, planes, s);
+    if (w == 64) return launch_piv_fp32_w64(p, dtype, mode, limit, planes, s);
     return cudaErrorInvalidValue;
 }
 

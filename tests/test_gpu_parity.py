@@ -81,7 +81,7 @@ def test_exact_planes_bit_identical(orc, w, mode):
         assert np.array_equal(got[k], ref), f"window {k}: max diff {np.abs(got[k] - ref).max()}"
 
 
-@pytest.mark.parametrize("w", [16, 32])
+@pytest.mark.parametrize("w", [16, 32, 64])
 @pytest.mark.parametrize("mode", [og.CORR_REAL, og.CORR_COMPLEX])
 def test_fp32_planes_within_tolerance(orc, w, mode):
     rng = np.random.default_rng(200 + w + mode)
@@ -159,6 +159,16 @@ def test_w16_uint16(orc):
         for limit in (False, True):
             vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 16, 4, mode, limit)
             assert_vectors_match(vec, pk, ref_vec, ref_pk, 16, f"w16 {mode} {limit}")
+
+
+def test_w64_uint16(orc):
+    """64 x 64 windows (the shared-memory kernel) at step 16 and step 24."""
+    a, b = synth.config2(size=1024)
+    for step in (16, 24):
+        for mode in (og.CORR_COMPLEX, og.CORR_REAL):
+            for limit in (False, True):
+                vec, pk, ref_vec, ref_pk, _ = run_both(orc, a, b, 64, step, mode, limit)
+                assert_vectors_match(vec, pk, ref_vec, ref_pk, 64, f"w64/{step} {mode} {limit}")
 
 
 def test_float32_frames(orc):
