@@ -124,6 +124,36 @@ int64_t opiv_plan_exact_count(opiv_plan* plan);
 int opiv_plan_set_timing(opiv_plan* plan, int enable);
 int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
 
+/* ---- multi-pass window offsetting ------------------------------------------
+ * No counterpart in the reference (its README lists multi-pass as to do,
+ * README.md:280); composed from the reference's per-window steps.  Pass 0 is
+ * the single pass above.  Pass k > 0 (window ia[k], step step[k]) moves every
+ * frame-B window by the integer displacement of the previous pass's window
+ * whose centre is nearest, clamped to keep the window inside the image, then
+ * correlates, searches and fits as usual; its vector is the residual vector
+ * minus that offset, so it is the total displacement in the reference's
+ * sign convention.  The integer displacement a window hands on is its
+ * offset plus (px - W/2, py - W/2) of its first peak, or its offset when it
+ * has fewer than two peaks; packed (dy << 16) | (dx & 0xffff). */
+typedef struct opiv_multipass opiv_multipass;
+int opiv_multipass_create(opiv_multipass** mp, uint32_t img_w, uint32_t img_h, int dtype,
+                          int n_passes, const uint32_t* ia, const uint32_t* step, int mode,
+                          int limit_search, int device);
+int opiv_multipass_destroy(opiv_multipass* mp);
+int64_t opiv_multipass_window_count(const opiv_multipass* mp, int pass);
+int opiv_multipass_grid(const opiv_multipass* mp, int pass, int32_t* out_xy, int64_t cap);
+/* host frames in; the last pass's vectors / peak codes / displacements out
+ * (each may be NULL); every pass's results stay readable with _results */
+int opiv_multipass_process(opiv_multipass* mp, const void* frame_a, const void* frame_b,
+                           size_t pitch_bytes, opiv_vector* out_vec, int32_t* out_peak,
+                           int32_t* out_disp);
+/* device frames, asynchronous on `stream`; results stay on the device */
+int opiv_multipass_process_device(opiv_multipass* mp, const void* d_frame_a, const void* d_frame_b,
+                                  size_t pitch_bytes, void* stream);
+/* copies pass `pass`'s results to host buffers (synchronises the device) */
+int opiv_multipass_results(opiv_multipass* mp, int pass, opiv_vector* out_vec, int32_t* out_peak,
+                           int32_t* out_disp);
+
 /* ---- allocation-free pass ------------------------------------------------ */
 /* No counterpart in the reference.  The same pass as opiv_process_pair_device
  * for callers that must not allocate device memory once they are running

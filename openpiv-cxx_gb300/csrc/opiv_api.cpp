@@ -134,6 +134,16 @@ struct opiv_plan {
     unsigned int* h_flag_count = nullptr;   // pinned copy of the last count
     bool timing = false;
     cudaEvent_t ev[3] = { nullptr, nullptr, nullptr };   // fp32 start, fp32 end, exact end
+    int32_t* d_disp = nullptr;          // integer displacements (multi-pass plans)
+};
+
+// A chain of plans over the same image pair: pass k's frame-B windows are
+// offset by pass k-1's integer displacements (offsets.cuh).
+struct opiv_multipass {
+    std::vector<opiv_plan*> passes;
+    void* d_fa = nullptr;
+    void* d_fb = nullptr;
+    size_t d_pitch = 0;
 };
 
 namespace {
@@ -152,6 +162,7 @@ void plan_free(opiv_plan* p)
     cudaFree(p->d_flag_count);
     cudaFree(p->d_flag_list);
     cudaFree(p->d_tw);
+    cudaFree(p->d_disp);
     if (p->h_flag_count) cudaFreeHost(p->h_flag_count);
     for (cudaEvent_t& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -180,9 +191,10 @@ PivParams base_params(const opiv_plan* p)
 }
 
 // One pass: FP32 kernel over all windows, then the exact pass over the
-// flagged ones.  Two kernel launches.
+// flagged ones.  Two kernel launches.  `prev` (may be null): the previous
+// pass of a multi-pass chain, whose integer displacements offset frame B.
 int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_vector* vec,
-             int32_t* peak, cudaStream_t s)
+             int32_t* peak, cudaStream_t s, const opiv_plan* prev = nullptr)
 {
     PivParams k = base_params(p);
     k.fa = fa;
@@ -190,6 +202,17 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
     k.pitch = pitch;
     k.out_vec = vec;
     k.out_peak = peak;
+    k.out_disp = p->d_disp;
+    if (prev != nullptr) {
+        k.prev_disp = prev->d_disp;
+        k.pgx0 = (int)prev->g.xs;
+        k.pgy0 = (int)prev->g.ys;
+        k.pgdx = (int)prev->dx;
+        k.pgdy = (int)prev->dy;
+        k.pgnx = (int)prev->g.xc;
+        k.pgny = (int)prev->g.yc;
+        k.pw = (int)prev->ia;
+    }
     CUDA_TRY(cudaMemsetAsync(p->d_flag_count, 0, sizeof(unsigned int), s));
     if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
     CUDA_TRY(launch_piv_fp32(k, (int)p->ia, p->dtype, p->mode, p->limit, false, s));
@@ -420,6 +443,142 @@ int64_t opiv_plan_exact_count(opiv_plan* plan)
     if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
     cudaDeviceSynchronize();
     return (int64_t)*plan->h_flag_count;
+}
+
+int opiv_multipass_create(opiv_multipass** out, uint32_t img_w, uint32_t img_h, int dtype,
+                          int n_passes, const uint32_t* ia, const uint32_t* step, int mode,
+                          int limit_search, int device)
+{
+    if (!out || !ia || !step || n_passes < 1) return fail(OPIV_ERR_ARG, "invalid multi-pass arguments");
+    *out = nullptr;
+    opiv_multipass* mp = new (std::nothrow) opiv_multipass;
+    if (!mp) return fail(OPIV_ERR_ARG, "out of host memory");
+    for (int k = 0; k < n_passes; ++k) {
+        opiv_plan* p = nullptr;
+        int rc = opiv_plan_create(&p, img_w, img_h, dtype, ia[k], step[k], step[k], mode,
+                                  limit_search, device);
+        if (rc == OPIV_OK) {
+            int prev = 0;
+            cudaGetDevice(&prev);
+            cudaSetDevice(device);
+            const cudaError_t e = cudaMalloc(&p->d_disp, sizeof(int32_t) * p->n_win);
+            cudaSetDevice(prev);
+            if (e != cudaSuccess) {
+                plan_free(p);
+                rc = cuda_fail(e, "cudaMalloc(displacements)");
+            }
+        }
+        if (rc != OPIV_OK) {
+            opiv_multipass_destroy(mp);
+            return rc;
+        }
+        mp->passes.push_back(p);
+    }
+    *out = mp;
+    return OPIV_OK;
+}
+
+int opiv_multipass_destroy(opiv_multipass* mp)
+{
+    if (!mp) return OPIV_OK;
+    if (!mp->passes.empty()) {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(mp->passes[0]->device);
+        cudaFree(mp->d_fa);
+        cudaFree(mp->d_fb);
+        cudaSetDevice(prev);
+    }
+    for (opiv_plan* p : mp->passes) plan_free(p);
+    delete mp;
+    return OPIV_OK;
+}
+
+int64_t opiv_multipass_window_count(const opiv_multipass* mp, int pass)
+{
+    if (!mp || pass < 0 || pass >= (int)mp->passes.size()) return fail(OPIV_ERR_ARG, "no such pass");
+    return mp->passes[pass]->n_win;
+}
+
+int opiv_multipass_grid(const opiv_multipass* mp, int pass, int32_t* out_xy, int64_t cap)
+{
+    if (!mp || pass < 0 || pass >= (int)mp->passes.size()) return fail(OPIV_ERR_ARG, "no such pass");
+    return opiv_plan_grid(mp->passes[pass], out_xy, cap);
+}
+
+int opiv_multipass_process_device(opiv_multipass* mp, const void* d_fa, const void* d_fb,
+                                  size_t pitch_bytes, void* stream)
+{
+    if (!mp || !d_fa || !d_fb) return fail(OPIV_ERR_ARG, "null argument");
+    opiv_plan* first = mp->passes[0];
+    if (pitch_bytes < (size_t)first->img_w * px_bytes(first->dtype))
+        return fail(OPIV_ERR_ARG, "pitch %zu smaller than a row", pitch_bytes);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(first->device);
+    int rc = OPIV_OK;
+    for (size_t k = 0; k < mp->passes.size() && rc == OPIV_OK; ++k) {
+        opiv_plan* p = mp->passes[k];
+        rc = run_pass(p, d_fa, d_fb, pitch_bytes, p->d_vec, p->d_peak, (cudaStream_t)stream,
+                      k ? mp->passes[k - 1] : nullptr);
+    }
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int opiv_multipass_process(opiv_multipass* mp, const void* frame_a, const void* frame_b,
+                           size_t pitch_bytes, opiv_vector* out_vec, int32_t* out_peak,
+                           int32_t* out_disp)
+{
+    if (!mp || !frame_a || !frame_b) return fail(OPIV_ERR_ARG, "null argument");
+    opiv_plan* first = mp->passes[0];
+    const size_t row = (size_t)first->img_w * px_bytes(first->dtype);
+    if (pitch_bytes < row) return fail(OPIV_ERR_ARG, "pitch %zu smaller than a row", pitch_bytes);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(first->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaError_t e;
+    if (!mp->d_fa) {
+        if ((e = cudaMalloc(&mp->d_fa, row * first->img_h)) != cudaSuccess) return done(cuda_fail(e, "cudaMalloc(frame)"));
+        if ((e = cudaMalloc(&mp->d_fb, row * first->img_h)) != cudaSuccess) return done(cuda_fail(e, "cudaMalloc(frame)"));
+        mp->d_pitch = row;
+    }
+    cudaStream_t s = first->stream;
+    if ((e = cudaMemcpy2DAsync(mp->d_fa, mp->d_pitch, frame_a, pitch_bytes, row, first->img_h,
+                               cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy2DAsync(frame a)"));
+    if ((e = cudaMemcpy2DAsync(mp->d_fb, mp->d_pitch, frame_b, pitch_bytes, row, first->img_h,
+                               cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy2DAsync(frame b)"));
+    const int rc = opiv_multipass_process_device(mp, mp->d_fa, mp->d_fb, mp->d_pitch, s);
+    if (rc != OPIV_OK) return done(rc);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return done(cuda_fail(e, "cudaStreamSynchronize"));
+    cudaSetDevice(prev);
+    return opiv_multipass_results(mp, (int)mp->passes.size() - 1, out_vec, out_peak, out_disp);
+}
+
+int opiv_multipass_results(opiv_multipass* mp, int pass, opiv_vector* out_vec, int32_t* out_peak,
+                           int32_t* out_disp)
+{
+    if (!mp || pass < 0 || pass >= (int)mp->passes.size()) return fail(OPIV_ERR_ARG, "no such pass");
+    opiv_plan* p = mp->passes[pass];
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(p->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaError_t e;
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return done(cuda_fail(e, "cudaDeviceSynchronize"));
+    if (out_vec && (e = cudaMemcpy(out_vec, p->d_vec, sizeof(opiv_vector) * p->n_win,
+                                   cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy(vectors)"));
+    if (out_peak && (e = cudaMemcpy(out_peak, p->d_peak, sizeof(int32_t) * p->n_win,
+                                    cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy(peaks)"));
+    if (out_disp && (e = cudaMemcpy(out_disp, p->d_disp, sizeof(int32_t) * p->n_win,
+                                    cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaMemcpy(displacements)"));
+    return done(OPIV_OK);
 }
 
 int opiv_plan_set_timing(opiv_plan* plan, int enable)

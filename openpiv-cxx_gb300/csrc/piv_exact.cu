@@ -27,6 +27,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "offsets.cuh"
 #include "piv_kernels.h"
 #include "sort_order.h"
 
@@ -153,14 +154,15 @@ piv_exact_kernel(const PivParams p, int W, int mode, int limit, bool use_list)
 
     for (int64_t item = blockIdx.x; item < nwork; item += gridDim.x) {
         const int64_t w = use_list ? (int64_t)p.flag_list[item] : item;
-        int bx, by;
+        int bx, by, ox, oy;
         window_origin(p, w, bx, by);
+        b_offset(p, W, bx, by, ox, oy);
 
         // ---- extract, convert (g_f by value), join / convert to complex
         for (int i = t; i < N; i += blockDim.x) {
             const int y = i / W, x = i % W;
             const double a = px_d(fa + (size_t)(by + y) * pitch + bx + x);
-            const double b = px_d(fb + (size_t)(by + y) * pitch + bx + x);
+            const double b = px_d(fb + (size_t)(by + oy + y) * pitch + bx + ox + x);
             if (mode == kModeComplex) {
                 A[i] = make_double2(a, 0.0);
                 B[i] = make_double2(b, 0.0);
@@ -272,13 +274,16 @@ piv_exact_kernel(const PivParams p, int W, int mode, int limit, bool use_list)
                 const int mx = bx + W / 2, my = by + W / 2;
                 out.x = (float)mx;
                 out.y = (float)((double)p.img_h - (double)my);
-                out.u = (float)((double)mx - ((double)bx + lx));
-                out.v = (float)((double)my - ((double)by + ly));
+                out.u = (float)((double)mx - ((double)bx + lx) - (double)ox);
+                out.v = (float)((double)my - ((double)by + ly) - (double)oy);
                 out.sn = (g1 > 0) ? (float)(g0 / g1) : 0.f;
                 code = k | OPIV_PEAK_EXACT;
             }
             if (p.out_vec) p.out_vec[w] = out;
             if (p.out_peak) p.out_peak[w] = code;
+            if (p.out_disp)
+                p.out_disp[w] = count == 2 ? pack_disp(k % W - W / 2 + ox, k / W - W / 2 + oy)
+                                           : pack_disp(ox, oy);
         }
         __syncthreads();
     }

@@ -44,6 +44,7 @@
 #include <cuda_runtime.h>
 
 #include "fft_reg.cuh"
+#include "offsets.cuh"
 #include "piv_kernels.h"
 
 namespace opiv {
@@ -206,11 +207,15 @@ piv_fp32_kernel(const PivParams p)
         if (st == kStLoad0 || st == kStLoad1) {
             // extract + widen: lane = row y, registers = x
             if (valid) {
-                int bx, by;
+                int bx, by, ox, oy;
                 window_origin(p, w, bx, by);
+                b_offset(p, W, bx, by, ox, oy);
                 const size_t off = (size_t)(by + gl) * pitch + bx;
                 load_row<W, false, PixT, VEC>(fa + off, v);
-                load_row<W, true, PixT, VEC>(fb + off, v);
+                if (p.prev_disp != nullptr)   // shifted B rows need not be aligned
+                    load_row<W, true, PixT, false>(fb + (size_t)(by + oy + gl) * pitch + bx + ox, v);
+                else
+                    load_row<W, true, PixT, VEC>(fb + off, v);
                 if (PLANES) {   // exact pedestal for the per-window API (double input)
                     double sa = 0.0, sb = 0.0;
 #pragma unroll 4
@@ -393,6 +398,9 @@ piv_fp32_kernel(const PivParams p)
             bool certain;
             opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
             int32_t code = -1;
+            int bx, by, ox, oy;
+            window_origin(p, w, bx, by);
+            b_offset(p, W, bx, by, ox, oy);
             if (!has2) {
                 certain = !(umax > kNegInf);
             } else {
@@ -421,17 +429,17 @@ piv_fp32_kernel(const PivParams p)
                 certain = (umax < t1 - 2.f * dlt) && (t0 - t1 > dlt) && (fabsf(p1) > dlt) &&
                           (ex < kFitTol) && (ey < kFitTol) &&
                           (p1 <= 0.f || sn_err < kSnTol * (1.f + p0 / p1));
-                int bx, by;
-                window_origin(p, w, bx, by);
                 out.x = (float)(bx + W / 2);
                 out.y = (float)(p.img_h - (by + W / 2));
-                out.u = (float)(W / 2 - px) - fx;
-                out.v = (float)(W / 2 - py) - fy;
+                out.u = (float)(W / 2 - px - ox) - fx;
+                out.v = (float)(W / 2 - py - oy) - fy;
                 out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
                 code = key;
             }
             p.out_vec[w] = out;
             if (p.out_peak) p.out_peak[w] = code;
+            if (p.out_disp)
+                p.out_disp[w] = has2 ? pack_disp(px - W / 2 + ox, py - W / 2 + oy) : pack_disp(ox, oy);
             if (!certain && p.flag_list) {
                 const unsigned int slot = atomicAdd(p.flag_count, 1u);
                 p.flag_list[slot] = (int32_t)w;

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "fft_reg.cuh"
+#include "offsets.cuh"
 #include "piv_kernels.h"
 
 namespace opiv {
@@ -137,19 +138,23 @@ piv_w64_kernel(const PivParams p)
     const size_t pitch = p.pitch / sizeof(PixT);
 
     // ---- extract, widen, energies (and the exact pedestal for the batch API)
-    int bx0, by0, bx1 = 0, by1 = 0;
+    int bx0, by0, bx1 = 0, by1 = 0, ox0, oy0, ox1 = 0, oy1 = 0;
     window_origin(p, w0, bx0, by0);
-    if (valid1) window_origin(p, w1, bx1, by1);
+    b_offset(p, W, bx0, by0, ox0, oy0);
+    if (valid1) {
+        window_origin(p, w1, bx1, by1);
+        b_offset(p, W, bx1, by1, ox1, oy1);
+    }
     float e0 = 0.f, e1 = 0.f;
     double sa0 = 0.0, sb0 = 0.0, sa1 = 0.0, sb1 = 0.0;
     for (int i = t; i < N; i += kThreads) {
         const int y = i >> 6, x = i & 63;
         const double a0 = (double)__ldg(fa + (size_t)(by0 + y) * pitch + bx0 + x);
-        const double b0 = (double)__ldg(fb + (size_t)(by0 + y) * pitch + bx0 + x);
+        const double b0 = (double)__ldg(fb + (size_t)(by0 + oy0 + y) * pitch + bx0 + ox0 + x);
         double a1 = 0.0, b1 = 0.0;
         if (valid1) {
             a1 = (double)__ldg(fa + (size_t)(by1 + y) * pitch + bx1 + x);
-            b1 = (double)__ldg(fb + (size_t)(by1 + y) * pitch + bx1 + x);
+            b1 = (double)__ldg(fb + (size_t)(by1 + oy1 + y) * pitch + bx1 + ox1 + x);
         }
         const float2 z0 = make_float2((float)a0, (float)b0), z1 = make_float2((float)a1, (float)b1);
         T1[y * LD + x] = z0;
@@ -316,13 +321,18 @@ piv_w64_kernel(const PivParams p)
                     const int bx = h ? bx1 : bx0, by = h ? by1 : by0;
                     out.x = (float)(bx + W / 2);
                     out.y = (float)(p.img_h - (by + W / 2));
-                    out.u = (float)(W / 2 - px) - fx;
-                    out.v = (float)(W / 2 - py) - fy;
+                    out.u = (float)(W / 2 - px - (h ? ox1 : ox0)) - fx;
+                    out.v = (float)(W / 2 - py - (h ? oy1 : oy0)) - fy;
                     out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
                     code = gk;
                 }
                 p.out_vec[w] = out;
                 if (p.out_peak) p.out_peak[w] = code;
+                if (p.out_disp) {
+                    const int ox = h ? ox1 : ox0, oy = h ? oy1 : oy0;
+                    p.out_disp[w] = code >= 0 ? pack_disp(gk % W - W / 2 + ox, gk / W - W / 2 + oy)
+                                              : pack_disp(ox, oy);
+                }
                 if (!certain && p.flag_list) {
                     const unsigned int slot = atomicAdd(p.flag_count, 1u);
                     p.flag_list[slot] = (int32_t)w;

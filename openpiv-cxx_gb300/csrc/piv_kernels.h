@@ -33,6 +33,13 @@ struct PivParams {
     // exact pass
     const double2* tw_fwd = nullptr;   // reference twiddle tables for length W
     const double2* tw_rev = nullptr;
+    // window offsetting (multi-pass): integer displacement of every window
+    // of the previous pass, packed (dy << 16) | (dx & 0xffff), and that
+    // pass's grid; frame B's window is moved by the displacement of the
+    // previous window nearest to this window's centre.  Null: no offset.
+    const int32_t* prev_disp = nullptr;
+    int pgx0 = 0, pgy0 = 0, pgdx = 1, pgdy = 1, pgnx = 1, pgny = 1, pw = 0;
+    int32_t* out_disp = nullptr;       // this pass's integer displacements (may be null)
 };
 
 // Fused FP32 kernels, one entry per window size (piv_fp32_w*.cu; 64 x 64

@@ -47,6 +47,9 @@ SYMBOLS = [
     "opiv_plan_last_timing", "opiv_cross_correlate_batch",
     "opiv_find_peaks", "opiv_fit_simple_gaussian", "opiv_process_pair_device_noalloc",
     "opiv_image_info", "opiv_image_load", "opiv_vectors_write",
+    "opiv_multipass_create", "opiv_multipass_destroy", "opiv_multipass_window_count",
+    "opiv_multipass_grid", "opiv_multipass_process", "opiv_multipass_process_device",
+    "opiv_multipass_results",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -110,6 +113,18 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_image_load.argtypes = [C.c_char_p, C.c_void_p, C.c_size_t, C.c_uint32, C.c_uint32,
                                   C.c_int]
     L.opiv_vectors_write.argtypes = [C.c_char_p, C.c_void_p, C.c_int64]
+    L.opiv_multipass_create.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_int,
+                                        C.c_int, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                        C.c_int, C.c_int, C.c_int]
+    L.opiv_multipass_destroy.argtypes = [C.c_void_p]
+    L.opiv_multipass_window_count.restype = C.c_int64
+    L.opiv_multipass_window_count.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_multipass_grid.argtypes = [C.c_void_p, C.c_int, _ip, C.c_int64]
+    L.opiv_multipass_process.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+    L.opiv_multipass_process_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                                C.c_void_p]
+    L.opiv_multipass_results.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -222,6 +237,72 @@ class Plan:
         a, b = C.c_float(), C.c_float()
         _check(load().opiv_plan_last_timing(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+
+# ---- multi-pass window offsetting ------------------------------------------
+def unpack_disp(d: np.ndarray) -> np.ndarray:
+    """(n,) packed (dy << 16) | (dx & 0xffff) -> (n, 2) int (dx, dy)."""
+    d = np.asarray(d, np.int32)
+    return np.stack([(d & 0xFFFF).astype(np.uint16).astype(np.int16).astype(np.int64),
+                     (d >> 16).astype(np.int64)], 1)
+
+
+class MultiPass:
+    """A chain of passes (window sizes / steps) over one image pair; pass k's
+    frame-B windows are offset by pass k-1's integer displacements."""
+
+    def __init__(self, img_w: int, img_h: int, dtype, passes, mode: int = CORR_COMPLEX,
+                 limit_search: bool = False, device: int = 0):
+        L = load()
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in DTYPES:
+            raise OpivError(ERR_ARG, f"unsupported pixel type {self.dtype}")
+        ia = (C.c_uint32 * len(passes))(*[p[0] for p in passes])
+        st = (C.c_uint32 * len(passes))(*[p[1] for p in passes])
+        h = C.c_void_p()
+        _check(L.opiv_multipass_create(C.byref(h), img_w, img_h, DTYPES[self.dtype], len(passes),
+                                       ia, st, mode, int(bool(limit_search)), device))
+        self._h = h
+        self.passes = list(passes)
+        self.img_w, self.img_h = img_w, img_h
+        self.counts = [int(L.opiv_multipass_window_count(h, k)) for k in range(len(passes))]
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().opiv_multipass_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def grid(self, k: int) -> np.ndarray:
+        out = np.zeros((self.counts[k], 2), np.int32)
+        _check(load().opiv_multipass_grid(self._h, k, out.ctypes.data_as(_ip), self.counts[k]))
+        return out
+
+    def process(self, frame_a: np.ndarray, frame_b: np.ndarray):
+        """Runs every pass; returns the last pass's (vectors, peak codes, displacements)."""
+        fa = np.ascontiguousarray(frame_a, self.dtype)
+        fb = np.ascontiguousarray(frame_b, self.dtype)
+        n = self.counts[-1]
+        vec = np.zeros((n, 5), np.float32)
+        pk = np.zeros(n, np.int32)
+        disp = np.zeros(n, np.int32)
+        _check(load().opiv_multipass_process(self._h, fa.ctypes.data, fb.ctypes.data, fa.strides[0],
+                                             vec.ctypes.data, pk.ctypes.data, disp.ctypes.data))
+        return vec, pk, unpack_disp(disp)
+
+    def results(self, k: int):
+        n = self.counts[k]
+        vec = np.zeros((n, 5), np.float32)
+        pk = np.zeros(n, np.int32)
+        disp = np.zeros(n, np.int32)
+        _check(load().opiv_multipass_results(self._h, k, vec.ctypes.data, pk.ctypes.data,
+                                             disp.ctypes.data))
+        return vec, pk, unpack_disp(disp)
 
 
 # ---- allocation-free pass --------------------------------------------------

@@ -240,15 +240,17 @@ void dilate_half(uint32_t w, uint32_t h, uint32_t* x0, uint32_t* y0, uint32_t* v
 
 // One window of examples/process/main.cpp:189-237.  vec = {x, y, u, v, sn};
 // pk = {px, py} of the first peak, or {-1, -1} when fewer than two peaks.
+// Frame B's window is extracted at (bbx, bby) (equal to (bx, by) in a single
+// pass; offset in a multi-pass chain); the vector refers to frame A's rect.
 void process_window(fft_ctx& c, const double* img_a, const double* img_b, uint32_t img_w,
-                    uint32_t img_h, int32_t bx, int32_t by, int mode, int limit_search,
-                    std::vector<double>& wa, std::vector<double>& wb, std::vector<double>& plane,
-                    double* vec, int32_t* pk)
+                    uint32_t img_h, int32_t bx, int32_t by, int32_t bbx, int32_t bby, int mode,
+                    int limit_search, std::vector<double>& wa, std::vector<double>& wb,
+                    std::vector<double>& plane, double* vec, int32_t* pk)
 {
     const uint32_t W = c.w, H = c.h;
     for (uint32_t y = 0; y < H; ++y) {   // core::extract, image_utils.impl.h:392-419
         std::memcpy(&wa[(size_t)y * W], img_a + (size_t)(by + y) * img_w + bx, sizeof(double) * W);
-        std::memcpy(&wb[(size_t)y * W], img_b + (size_t)(by + y) * img_w + bx, sizeof(double) * W);
+        std::memcpy(&wb[(size_t)y * W], img_b + (size_t)(bby + y) * img_w + bbx, sizeof(double) * W);
     }
     cross_correlate(c, wa.data(), wb.data(), mode, plane.data());
     uint32_t x0 = 0, y0 = 0, vw = W, vh = H;
@@ -395,15 +397,43 @@ int orc_correlate_windows(const double* img_a, const double* img_b, uint32_t img
 // "pool" execution, main.cpp:265-276).  Returns the processing time in
 // seconds (timing covers the loop only, as main.cpp:239/304 does), or a
 // negative error code.
+static double process_windows_impl(const double* img_a, const double* img_b, uint32_t img_w,
+                                   uint32_t img_h, const int32_t* win_xy, const int32_t* win_b,
+                                   int64_t n, uint32_t w, int mode, int limit_search, int threads,
+                                   double* out_vec, int32_t* out_peak);
+
 double orc_process_windows(const double* img_a, const double* img_b, uint32_t img_w,
                            uint32_t img_h, const int32_t* win_xy, int64_t n, uint32_t w, int mode,
                            int limit_search, int threads, double* out_vec, int32_t* out_peak)
 {
+    return process_windows_impl(img_a, img_b, img_w, img_h, win_xy, nullptr, n, w, mode,
+                                limit_search, threads, out_vec, out_peak);
+}
+
+// Same with frame B's windows at their own corners win_b (multi-pass
+// window offsetting, composed from the same reference steps).
+double orc_process_windows_ab(const double* img_a, const double* img_b, uint32_t img_w,
+                              uint32_t img_h, const int32_t* win_xy, const int32_t* win_b,
+                              int64_t n, uint32_t w, int mode, int limit_search, int threads,
+                              double* out_vec, int32_t* out_peak)
+{
+    return process_windows_impl(img_a, img_b, img_w, img_h, win_xy, win_b, n, w, mode,
+                                limit_search, threads, out_vec, out_peak);
+}
+
+static double process_windows_impl(const double* img_a, const double* img_b, uint32_t img_w,
+                                   uint32_t img_h, const int32_t* win_xy, const int32_t* win_b,
+                                   int64_t n, uint32_t w, int mode, int limit_search, int threads,
+                                   double* out_vec, int32_t* out_peak)
+{
     if (!is_pow2(w)) return ORC_ERR_NOT_POW2;
     for (int64_t k = 0; k < n; ++k) {
-        const int32_t bx = win_xy[2 * k], by = win_xy[2 * k + 1];
-        if (bx < 0 || by < 0 || (uint32_t)bx + w > img_w || (uint32_t)by + w > img_h)
-            return ORC_ERR_RECT_OUTSIDE;
+        for (const int32_t* xy : { win_xy, win_b }) {
+            if (!xy) continue;
+            const int32_t bx = xy[2 * k], by = xy[2 * k + 1];
+            if (bx < 0 || by < 0 || (uint32_t)bx + w > img_w || (uint32_t)by + w > img_h)
+                return ORC_ERR_RECT_OUTSIDE;
+        }
     }
     std::atomic<int64_t> next{ 0 };
     auto worker = [&]() {
@@ -412,8 +442,10 @@ double orc_process_windows(const double* img_a, const double* img_b, uint32_t im
         for (;;) {
             const int64_t k = next.fetch_add(1, std::memory_order_relaxed);
             if (k >= n) break;
-            process_window(c, img_a, img_b, img_w, img_h, win_xy[2 * k], win_xy[2 * k + 1], mode,
-                           limit_search, wa, wb, plane, out_vec + 5 * k, out_peak + 2 * k);
+            const int32_t* bxy = win_b ? win_b : win_xy;
+            process_window(c, img_a, img_b, img_w, img_h, win_xy[2 * k], win_xy[2 * k + 1],
+                           bxy[2 * k], bxy[2 * k + 1], mode, limit_search, wa, wb, plane,
+                           out_vec + 5 * k, out_peak + 2 * k);
         }
     };
     const auto t1 = std::chrono::steady_clock::now();

@@ -67,6 +67,9 @@ class Oracle:
         L.orc_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_int32, C.c_int32, _dp]
         L.orc_correlate_windows.argtypes = [_dp, _dp, C.c_uint32, C.c_uint32, _ip, C.c_int64,
                                             C.c_uint32, C.c_int, _dp]
+        L.orc_process_windows_ab.restype = C.c_double
+        L.orc_process_windows_ab.argtypes = [_dp, _dp, C.c_uint32, C.c_uint32, _ip, _ip, C.c_int64,
+                                             C.c_uint32, C.c_int, C.c_int, C.c_int, _dp, _ip]
         L.orc_process_windows.restype = C.c_double
         L.orc_process_windows.argtypes = [_dp, _dp, C.c_uint32, C.c_uint32, _ip, C.c_int64,
                                           C.c_uint32, C.c_int, C.c_int, C.c_int, _dp, _ip]
@@ -173,6 +176,69 @@ class Oracle:
         if t < 0:
             raise RuntimeError(f"orc_process_windows: {t}")
         return vec, pk, t
+
+
+    def process_windows_ab(self, img_a, img_b, win_xy, win_b, w, mode, limit_search=False,
+                           threads=1):
+        """As process_windows, frame B's windows at their own corners."""
+        img_a = np.ascontiguousarray(img_a, np.float64)
+        img_b = np.ascontiguousarray(img_b, np.float64)
+        win_xy = np.ascontiguousarray(win_xy, np.int32)
+        win_b = np.ascontiguousarray(win_b, np.int32)
+        n = win_xy.shape[0]
+        vec = np.zeros((n, 5), np.float64)
+        pk = np.zeros((n, 2), np.int32)
+        t = self.lib.orc_process_windows_ab(img_a.ctypes.data_as(_dp), img_b.ctypes.data_as(_dp),
+                                            img_a.shape[1], img_a.shape[0],
+                                            win_xy.ctypes.data_as(_ip), win_b.ctypes.data_as(_ip),
+                                            n, w, mode, int(bool(limit_search)), int(threads),
+                                            vec.ctypes.data_as(_dp), pk.ctypes.data_as(_ip))
+        if t < 0:
+            raise RuntimeError(f"orc_process_windows_ab: {t}")
+        return vec, pk, t
+
+
+def nearest_index(c, c0, step, n):
+    """Index of the grid line (origin c0, spacing step, n lines) nearest to c:
+    floor((c - c0 + step/2) / step) clamped to [0, n - 1] (integer maths)."""
+    c = np.asarray(c, np.int64)
+    i = np.where(c < c0, 0, (c - c0 + step // 2) // step)
+    return np.minimum(i, n - 1)
+
+
+def multipass(orc, img_a, img_b, passes, mode, limit_search=False, threads=1):
+    """The multi-pass window-offsetting chain composed from the reference's
+    per-window steps.  passes: [(ia, step), ...].  Returns, per pass, a dict
+    with the grid, the B corners, the vectors (total displacement, the
+    reference's sign convention), the first-peak positions and the integer
+    displacements handed to the next pass."""
+    h, w = img_a.shape
+    fa, fb = np.asarray(img_a, np.float64), np.asarray(img_b, np.float64)
+    out, prev = [], None
+    for ia, step in passes:
+        grid = orc.grid_offsets(w, h, ia, ia, step, step)
+        bx, by = grid[:, 0].astype(np.int64), grid[:, 1].astype(np.int64)
+        ox = np.zeros(len(grid), np.int64)
+        oy = np.zeros(len(grid), np.int64)
+        if prev is not None:
+            pg, pdisp, pia, pstep = prev
+            pnx = len(np.unique(pg[:, 0]))
+            pny = len(pg) // pnx
+            ix = nearest_index(bx + ia // 2, pg[0, 0] + pia // 2, pstep, pnx)
+            iy = nearest_index(by + ia // 2, pg[0, 1] + pia // 2, pstep, pny)
+            d = pdisp[iy * pnx + ix]
+            ox = np.clip(d[:, 0], -bx, w - ia - bx)
+            oy = np.clip(d[:, 1], -by, h - ia - by)
+        bxy = np.stack([bx + ox, by + oy], 1).astype(np.int32)
+        vec, pk, _ = orc.process_windows_ab(fa, fb, grid, bxy, ia, mode, limit_search, threads)
+        found = pk[:, 0] >= 0
+        vec[found, 2] -= ox[found]
+        vec[found, 3] -= oy[found]
+        disp = np.stack([np.where(found, pk[:, 0] - ia // 2 + ox, ox),
+                         np.where(found, pk[:, 1] - ia // 2 + oy, oy)], 1)
+        out.append({"grid": grid, "b_xy": bxy, "vec": vec, "peak": pk, "disp": disp})
+        prev = (grid, disp, ia, step)
+    return out
 
 
 def get(kind: str = "port", fast: bool = False) -> Oracle:

@@ -193,9 +193,34 @@ int orc_correlate_windows(const double* img_a, const double* img_b, uint32_t img
 // reference API in the same order as its processor lambda, executed by the
 // example's own ThreadPool in "pool" mode (one task per window) when
 // threads > 1.  Returns the loop time in seconds.
+static double process_ab(const double* img_a, const double* img_b, uint32_t img_w, uint32_t img_h,
+                         const int32_t* win_xy, const int32_t* win_b, int64_t n, uint32_t w,
+                         int mode, int limit_search, int threads, double* out_vec,
+                         int32_t* out_peak);
+
 double orc_process_windows(const double* img_a, const double* img_b, uint32_t img_w,
                            uint32_t img_h, const int32_t* win_xy, int64_t n, uint32_t w, int mode,
                            int limit_search, int threads, double* out_vec, int32_t* out_peak)
+{
+    return process_ab(img_a, img_b, img_w, img_h, win_xy, nullptr, n, w, mode, limit_search,
+                      threads, out_vec, out_peak);
+}
+
+// Frame B's window extracted at its own rect (window offsetting composed
+// from the same reference calls: extract, correlator, find_peaks, fit).
+double orc_process_windows_ab(const double* img_a, const double* img_b, uint32_t img_w,
+                              uint32_t img_h, const int32_t* win_xy, const int32_t* win_b,
+                              int64_t n, uint32_t w, int mode, int limit_search, int threads,
+                              double* out_vec, int32_t* out_peak)
+{
+    return process_ab(img_a, img_b, img_w, img_h, win_xy, win_b, n, w, mode, limit_search,
+                      threads, out_vec, out_peak);
+}
+
+static double process_ab(const double* img_a, const double* img_b, uint32_t img_w, uint32_t img_h,
+                         const int32_t* win_xy, const int32_t* win_b, int64_t n, uint32_t w,
+                         int mode, int limit_search, int threads, double* out_vec,
+                         int32_t* out_peak)
 {
     std::vector<core::gf_image> images;
     images.push_back(from_buffer(img_a, img_w, img_h));
@@ -224,8 +249,9 @@ double orc_process_windows(const double* img_a, const double* img_b, uint32_t im
         int32_t* pk = out_peak + 2 * i;
         for (int j = 0; j < 5; ++j) vec[j] = 0.0;
         pk[0] = -1; pk[1] = -1;
+        const core::rect ib = win_b ? core::rect{ { win_b[2 * i], win_b[2 * i + 1] }, ia.size() } : ia;
         const auto view_a{ core::extract(images[0], ia) };
-        const auto view_b{ core::extract(images[1], ia) };
+        const auto view_b{ core::extract(images[1], ib) };
         const core::gf_image output{ correlator(view_a, view_b) };
         core::peaks_t<core::g_f> peaks;
         if (limit_search) {

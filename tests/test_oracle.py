@@ -178,3 +178,35 @@ def test_reference_rejects_non_square(ref_lib):
         ref_lib.transform_real(a, b)
     with pytest.raises(RuntimeError):
         ref_lib.transform(a + 0j, -1)
+
+
+def test_multipass_chain_vs_reference(orc, ref_lib):
+    """The window-offsetting chain (composed from reference calls) gives the
+    same result through the restatement and through the compiled reference."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(12)
+    a = rng.integers(0, 4096, (192, 256)).astype(np.float64)
+    b = np.roll(a, (-6, 9), (0, 1)) + rng.normal(0, 10, a.shape)
+    for mode in (0, 1):
+        r1 = O.multipass(orc, a, b, [(64, 32), (32, 16), (16, 8)], mode)
+        r2 = O.multipass(ref_lib, a, b, [(64, 32), (32, 16), (16, 8)], mode, threads=2)
+        for p1, p2 in zip(r1, r2):
+            assert np.array_equal(p1["disp"], p2["disp"])
+            assert np.array_equal(p1["peak"], p2["peak"])
+            assert np.array_equal(p1["vec"], p2["vec"], equal_nan=True)
+        ok = r1[-1]["peak"][:, 0] >= 0
+        hit = np.all(r1[-1]["disp"][ok] == [9, -6], axis=1)
+        assert hit.mean() > 0.9   # the shift, recovered at 16 px (edges wrap around)
+
+
+def test_nearest_index_rule():
+    from oracle import oracle as O
+    c0, step, n = 16, 16, 5          # centres 16, 32, 48, 64, 80
+    c = np.arange(0, 100)
+    centres = c0 + step * np.arange(n)
+    brute = np.array([np.argmin(np.abs(centres - x) + 1e-9 * np.arange(n)[::-1] * 0) for x in c])
+    got = O.nearest_index(c, c0, step, n)
+    # equidistant points (x = 24, 40, ...) go to the upper line: floor((d + 8) / 16)
+    ties = (c - c0) % step == step // 2
+    assert np.array_equal(got[~ties], brute[~ties])
+    assert np.all(got[ties & (c < 80)] == ((c[ties & (c < 80)] - c0) // step) + 1)
