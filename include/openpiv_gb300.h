@@ -48,7 +48,13 @@ enum {
 enum { OPIV_U8 = 0, OPIV_U16 = 1, OPIV_F32 = 2 };           /* pixel type of the frames */
 enum { OPIV_CORR_REAL = 0,      /* FFT::cross_correlate_real, fft.h:208-227 (spectrum row 0,
                                    row H/2 and column 0 left at zero, as the reference does) */
-       OPIV_CORR_COMPLEX = 1 }; /* FFT::cross_correlate, fft.h:188-206 (circular correlation) */
+       OPIV_CORR_COMPLEX = 1,   /* FFT::cross_correlate, fft.h:188-206 (circular correlation) */
+       OPIV_CORR_POCKET = 2,    /* PocketFFT::cross_correlate, pocket_fft.h:236-253: c2c both
+                                   ways with fct 1.0 -- the same circular correlation */
+       OPIV_CORR_POCKET_REAL = 3 }; /* PocketFFT::cross_correlate_real, pocket_fft.h:255-272:
+                                   r2c / c2r with fct 1.0 -- the same circular correlation
+                                   (no partial unpack); both pocket modes run the COMPLEX
+                                   kernels */
 
 /* Per-window result, as the reference's point_vector (main.cpp:144-149):
  * x, y   window midpoint, y measured from the image top (H - y, main.cpp:230)
@@ -153,6 +159,30 @@ int opiv_multipass_process_device(opiv_multipass* mp, const void* d_frame_a, con
 /* copies pass `pass`'s results to host buffers (synchronises the device) */
 int opiv_multipass_results(opiv_multipass* mp, int pass, opiv_vector* out_vec, int32_t* out_peak,
                            int32_t* out_disp);
+
+/* ---- batches of image pairs ------------------------------------------------
+ * No counterpart in the reference.  Many image pairs (each its own size)
+ * through the same multi-pass schedule.  The batch owns device frames
+ * (fill them with opiv_batch_upload or through opiv_batch_frames).
+ * opiv_batch_run enqueues every pair's passes on forked streams; with
+ * use_graph = 1 the first call records that whole submission into a CUDA
+ * graph (after one eager run) and every call replays the graph with one
+ * launch.  A null `stream` means the batch's own stream (used by
+ * opiv_batch_upload too).  Two kernel launches per pair and pass are added
+ * to opiv_kernel_launch_count for every run, replayed or not. */
+typedef struct opiv_batch opiv_batch;
+int opiv_batch_create(opiv_batch** batch, int n_pairs, const uint32_t* widths,
+                      const uint32_t* heights, int dtype, int n_passes, const uint32_t* ia,
+                      const uint32_t* step, int mode, int limit_search, int device);
+int opiv_batch_destroy(opiv_batch* batch);
+int opiv_batch_frames(opiv_batch* batch, int pair, void** d_frame_a, void** d_frame_b,
+                      size_t* pitch_bytes);
+int opiv_batch_upload(opiv_batch* batch, int pair, const void* frame_a, const void* frame_b,
+                      size_t pitch_bytes, void* stream);
+int opiv_batch_run(opiv_batch* batch, int use_graph, void* stream);
+int64_t opiv_batch_window_count(const opiv_batch* batch, int pair, int pass);
+int opiv_batch_results(opiv_batch* batch, int pair, int pass, opiv_vector* out_vec,
+                       int32_t* out_peak, int32_t* out_disp);
 
 /* ---- allocation-free pass ------------------------------------------------ */
 /* No counterpart in the reference.  The same pass as opiv_process_pair_device

@@ -102,6 +102,13 @@ std::vector<double2> reference_twiddles(uint32_t n, int dir)
 }
 
 constexpr int kExactBlocks = 152 * 2;   // CTAs of the exact pass (two per SM)
+
+// The PocketFFT modes compute the true circular correlation, as
+// FFT::cross_correlate does: they run the COMPLEX kernels.
+int kernel_mode(int mode)
+{
+    return (mode == OPIV_CORR_POCKET || mode == OPIV_CORR_POCKET_REAL) ? OPIV_CORR_COMPLEX : mode;
+}
 // Error-bound factor of the FP32 kernel: the largest error measured on 68k
 // windows of particle images (W = 16, 32; both modes) was 3.15 * 2^-24 * 2N *
 // (E_1 + E_2) (E = window energy of the pair sharing an inverse transform);
@@ -290,8 +297,9 @@ int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype,
     if (out == nullptr) return fail(OPIV_ERR_ARG, "plan pointer is null");
     *out = nullptr;
     if (px_bytes(dtype) == 0) return fail(OPIV_ERR_ARG, "unknown pixel type %d", dtype);
-    if (mode != OPIV_CORR_REAL && mode != OPIV_CORR_COMPLEX)
+    if (mode < OPIV_CORR_REAL || mode > OPIV_CORR_POCKET_REAL)
         return fail(OPIV_ERR_ARG, "unknown correlation mode %d", mode);
+    mode = kernel_mode(mode);
     grid_geom g;
     int rc = grid_geometry(img_w, img_h, ia, ia, dx, dy, g);
     if (rc != OPIV_OK) return rc;
@@ -581,6 +589,196 @@ int opiv_multipass_results(opiv_multipass* mp, int pass, opiv_vector* out_vec, i
     return done(OPIV_OK);
 }
 
+// ---- batches of image pairs ----------------------------------------------------
+struct opiv_batch {
+    std::vector<opiv_multipass*> pairs;
+    std::vector<void*> d_fa, d_fb;
+    std::vector<size_t> pitch;
+    cudaStream_t main = nullptr;         // used when the caller passes no stream
+    std::vector<cudaStream_t> streams;   // fork streams of the captured graph
+    std::vector<cudaEvent_t> events;     // fork / join events
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int device = 0;
+};
+
+int opiv_batch_destroy(opiv_batch* b)
+{
+    if (!b) return OPIV_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->main) cudaStreamSynchronize(b->main);
+    for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
+    if (b->main) cudaStreamDestroy(b->main);
+    for (cudaEvent_t ev : b->events) cudaEventDestroy(ev);
+    for (void* f : b->d_fa) cudaFree(f);
+    for (void* f : b->d_fb) cudaFree(f);
+    cudaSetDevice(prev);
+    for (opiv_multipass* mp : b->pairs) opiv_multipass_destroy(mp);
+    delete b;
+    return OPIV_OK;
+}
+
+int opiv_batch_create(opiv_batch** out, int n_pairs, const uint32_t* widths, const uint32_t* heights,
+                      int dtype, int n_passes, const uint32_t* ia, const uint32_t* step, int mode,
+                      int limit_search, int device)
+{
+    if (!out || n_pairs < 1 || !widths || !heights) return fail(OPIV_ERR_ARG, "invalid batch arguments");
+    *out = nullptr;
+    opiv_batch* b = new (std::nothrow) opiv_batch;
+    if (!b) return fail(OPIV_ERR_ARG, "out of host memory");
+    b->device = device;
+    for (int i = 0; i < n_pairs; ++i) {
+        opiv_multipass* mp = nullptr;
+        const int rc = opiv_multipass_create(&mp, widths[i], heights[i], dtype, n_passes, ia, step,
+                                             mode, limit_search, device);
+        if (rc != OPIV_OK) {
+            opiv_batch_destroy(b);
+            return rc;
+        }
+        b->pairs.push_back(mp);
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    cudaError_t e = cudaSuccess;
+    const int n_streams = n_pairs < 8 ? n_pairs : 8;
+    for (int i = 0; i < n_pairs && e == cudaSuccess; ++i) {
+        const size_t row = (size_t)widths[i] * px_bytes(dtype);
+        void *fa = nullptr, *fb = nullptr;
+        if ((e = cudaMalloc(&fa, row * heights[i])) != cudaSuccess) break;
+        b->d_fa.push_back(fa);
+        if ((e = cudaMalloc(&fb, row * heights[i])) != cudaSuccess) break;
+        b->d_fb.push_back(fb);
+        b->pitch.push_back(row);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreate(&b->main);
+    for (int i = 0; i < n_streams && e == cudaSuccess; ++i) {
+        cudaStream_t st;
+        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) break;
+        b->streams.push_back(st);
+    }
+    for (int i = 0; i < n_streams + 1 && e == cudaSuccess; ++i) {
+        cudaEvent_t ev;
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) break;
+        b->events.push_back(ev);
+    }
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        opiv_batch_destroy(b);
+        return cuda_fail(e, "opiv_batch_create");
+    }
+    *out = b;
+    return OPIV_OK;
+}
+
+int opiv_batch_frames(opiv_batch* b, int pair, void** d_frame_a, void** d_frame_b, size_t* pitch_bytes)
+{
+    if (!b || pair < 0 || pair >= (int)b->pairs.size() || !d_frame_a || !d_frame_b || !pitch_bytes)
+        return fail(OPIV_ERR_ARG, "no such pair");
+    *d_frame_a = b->d_fa[pair];
+    *d_frame_b = b->d_fb[pair];
+    *pitch_bytes = b->pitch[pair];
+    return OPIV_OK;
+}
+
+int opiv_batch_upload(opiv_batch* b, int pair, const void* frame_a, const void* frame_b,
+                      size_t pitch_bytes, void* stream)
+{
+    if (!b || pair < 0 || pair >= (int)b->pairs.size() || !frame_a || !frame_b)
+        return fail(OPIV_ERR_ARG, "no such pair");
+    const opiv_plan* p0 = b->pairs[pair]->passes[0];
+    const size_t row = (size_t)p0->img_w * px_bytes(p0->dtype);
+    if (pitch_bytes < row) return fail(OPIV_ERR_ARG, "pitch %zu smaller than a row", pitch_bytes);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->main;
+    cudaError_t e = cudaMemcpy2DAsync(b->d_fa[pair], b->pitch[pair], frame_a, pitch_bytes, row,
+                                      p0->img_h, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(b->d_fb[pair], b->pitch[pair], frame_b, pitch_bytes, row, p0->img_h,
+                              cudaMemcpyHostToDevice, s);
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? OPIV_OK : cuda_fail(e, "opiv_batch_upload");
+}
+
+namespace {
+
+// Every pair's pass chain, pairs spread over the fork streams.
+int batch_enqueue(opiv_batch* b, cudaStream_t s)
+{
+    const int ns = (int)b->streams.size();
+    CUDA_TRY(cudaEventRecord(b->events[ns], s));
+    for (int i = 0; i < ns; ++i) CUDA_TRY(cudaStreamWaitEvent(b->streams[i], b->events[ns], 0));
+    for (size_t i = 0; i < b->pairs.size(); ++i) {
+        const int rc = opiv_multipass_process_device(b->pairs[i], b->d_fa[i], b->d_fb[i], b->pitch[i],
+                                                     b->streams[i % ns]);
+        if (rc != OPIV_OK) return rc;
+    }
+    for (int i = 0; i < ns; ++i) {
+        CUDA_TRY(cudaEventRecord(b->events[i], b->streams[i]));
+        CUDA_TRY(cudaStreamWaitEvent(s, b->events[i], 0));
+    }
+    return OPIV_OK;
+}
+
+}  // namespace
+
+int opiv_batch_run(opiv_batch* b, int use_graph, void* stream)
+{
+    if (!b) return fail(OPIV_ERR_ARG, "batch is null");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->main;
+    if (!use_graph) return done(batch_enqueue(b, s));
+    cudaError_t e;
+    if (!b->exec) {
+        // one eager run first: one-time kernel attribute set-up happens
+        // outside the capture
+        int rc = batch_enqueue(b, s);
+        if (rc != OPIV_OK) return done(rc);
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return done(cuda_fail(e, "cudaStreamSynchronize"));
+        if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaStreamBeginCapture"));
+        const int64_t counted = g_launches;   // a capture launches nothing
+        rc = batch_enqueue(b, s);
+        g_launches = counted;
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(s, &g);
+        if (rc != OPIV_OK) {
+            if (g) cudaGraphDestroy(g);
+            return done(rc);
+        }
+        if (e != cudaSuccess) return done(cuda_fail(e, "cudaStreamEndCapture"));
+        b->graph = g;
+        if ((e = cudaGraphInstantiate(&b->exec, g, 0)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaGraphInstantiate"));
+        return done(OPIV_OK);   // the eager run has produced this call's results
+    }
+    if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return done(cuda_fail(e, "cudaGraphLaunch"));
+    g_launches += 2 * (int64_t)b->pairs.size() * (int64_t)b->pairs[0]->passes.size();
+    return done(OPIV_OK);
+}
+
+int64_t opiv_batch_window_count(const opiv_batch* b, int pair, int pass)
+{
+    if (!b || pair < 0 || pair >= (int)b->pairs.size()) return fail(OPIV_ERR_ARG, "no such pair");
+    return opiv_multipass_window_count(b->pairs[pair], pass);
+}
+
+int opiv_batch_results(opiv_batch* b, int pair, int pass, opiv_vector* out_vec, int32_t* out_peak,
+                       int32_t* out_disp)
+{
+    if (!b || pair < 0 || pair >= (int)b->pairs.size()) return fail(OPIV_ERR_ARG, "no such pair");
+    return opiv_multipass_results(b->pairs[pair], pass, out_vec, out_peak, out_disp);
+}
+
 int opiv_plan_set_timing(opiv_plan* plan, int enable)
 {
     if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
@@ -615,8 +813,9 @@ int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int
                                int exact, double* out_planes, int device)
 {
     if (!a || !b || !out_planes || n < 0) return fail(OPIV_ERR_ARG, "null argument");
-    if (mode != OPIV_CORR_REAL && mode != OPIV_CORR_COMPLEX)
+    if (mode < OPIV_CORR_REAL || mode > OPIV_CORR_POCKET_REAL)
         return fail(OPIV_ERR_ARG, "unknown correlation mode %d", mode);
+    mode = kernel_mode(mode);
     if (!is_pow2(w)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", w, w);
     if (exact ? !exact_supports((int)w) : !fp32_supports((int)w))
         return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", w, w);

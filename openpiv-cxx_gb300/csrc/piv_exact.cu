@@ -24,6 +24,7 @@
 // CTAs stride over the work list.  FP64 is slow on this part, so the hot path only sends
 // the rare flagged windows here.
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -294,9 +295,18 @@ cudaError_t launch_t(const PivParams& p, int w, int mode, int limit, bool use_li
                      cudaStream_t s)
 {
     const size_t smem = 2 * sizeof(double2) * (size_t)w * w;
-    cudaError_t e = cudaFuncSetAttribute(piv_exact_kernel<PixT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    // the opt-in limit for the largest window, once per device
+    static std::atomic<uint64_t> attr_done{ 0 };
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
+        const cudaError_t e = cudaFuncSetAttribute(piv_exact_kernel<PixT>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)(2 * sizeof(double2) * 64 * 64));
+        if (e != cudaSuccess) return e;
+        attr_done.fetch_or(bit);
+    }
     piv_exact_kernel<PixT><<<blocks, kThreads, smem, s>>>(p, w, mode, limit, use_list);
     return cudaGetLastError();
 }

@@ -40,6 +40,7 @@
 // windows are re-decided by the exact double-precision kernel
 // (piv_exact.cu), which overwrites their results.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -463,12 +464,16 @@ cudaError_t launch_t(const PivParams& p, cudaStream_t s)
     const size_t smem = sizeof(float2) * kWarps * NG * group_smem_float2<W>();
     auto kern = vec ? piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, true>
                     : piv_fp32_kernel<W, MODE, LIMIT, PixT, PLANES, false>;
-    static bool attr_done[2] = { false, false };   // per instantiation and load path
-    if (!attr_done[vec]) {
+    // per instantiation, load path and device
+    static std::atomic<uint64_t> attr_done[2] = { { 0 }, { 0 } };
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done[vec].load() & bit)) {
         const cudaError_t e =
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        attr_done[vec] = true;
+        attr_done[vec].fetch_or(bit);
     }
     kern<<<(unsigned)blocks, 32 * kWarps, smem, s>>>(p);
     return cudaGetLastError();

@@ -15,6 +15,7 @@
 //   reduction; fit_simple_gaussian (impl:77-101); vector of main.cpp:220-236;
 //   the same certification and hand-off to the exact kernel.
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -347,13 +348,16 @@ template <int MODE, bool LIMIT, typename PixT, bool PLANES>
 cudaError_t launch_t(const PivParams& p, cudaStream_t s)
 {
     const size_t smem = sizeof(float2) * 2 * W * LD;
-    static bool attr_done = false;
-    if (!attr_done) {
+    static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
         const cudaError_t e = cudaFuncSetAttribute(piv_w64_kernel<MODE, LIMIT, PixT, PLANES>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    (int)smem);
         if (e != cudaSuccess) return e;
-        attr_done = true;
+        attr_done.fetch_or(bit);
     }
     const int64_t blocks = (p.n_win + 1) / 2;
     piv_w64_kernel<MODE, LIMIT, PixT, PLANES><<<(unsigned)blocks, kThreads, smem, s>>>(p);

@@ -1,7 +1,8 @@
 // process_gb300 -- the reference's examples/process, with the per-window loop
 // (main.cpp:189-302) replaced by one GPU pass through the C ABI.
 //
-//   process_gb300 [-s size] [-o overlap] [-f complex|real] [-l] [-d device]
+//   process_gb300 [-s size] [-o overlap] [-f complex|real|pocket|pocket_real]
+//                 [-l] [-d device]
 //                 [-i] frame_a frame_b
 //
 // Same options and meaning as main.cpp:53-63: -s interrogation size
@@ -58,6 +59,8 @@ int main(int argc, char** argv)
     int mode;
     if (fft_type == "complex") mode = OPIV_CORR_COMPLEX;
     else if (fft_type == "real") mode = OPIV_CORR_REAL;
+    else if (fft_type == "pocket") mode = OPIV_CORR_POCKET;
+    else if (fft_type == "pocket_real") mode = OPIV_CORR_POCKET_REAL;
     else {
         std::cerr << "unknown fft type: " << fft_type << "\n";
         return 1;

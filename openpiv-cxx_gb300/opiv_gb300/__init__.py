@@ -19,7 +19,7 @@ PKG = os.path.dirname(HERE)
 LIB_PATH = os.path.join(PKG, "lib", "libopenpiv_gb300.so")
 
 U8, U16, F32 = 0, 1, 2
-CORR_REAL, CORR_COMPLEX = 0, 1
+CORR_REAL, CORR_COMPLEX, CORR_POCKET, CORR_POCKET_REAL = 0, 1, 2, 3
 PEAK_EXACT = 0x40000000
 PEAK_MASK = 0x0000FFFF
 
@@ -49,7 +49,8 @@ SYMBOLS = [
     "opiv_image_info", "opiv_image_load", "opiv_vectors_write",
     "opiv_multipass_create", "opiv_multipass_destroy", "opiv_multipass_window_count",
     "opiv_multipass_grid", "opiv_multipass_process", "opiv_multipass_process_device",
-    "opiv_multipass_results",
+    "opiv_multipass_results", "opiv_batch_create", "opiv_batch_destroy", "opiv_batch_frames",
+    "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -125,6 +126,20 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_multipass_process_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
                                                 C.c_void_p]
     L.opiv_multipass_results.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.opiv_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_uint32),
+                                    C.POINTER(C.c_uint32), C.c_int, C.c_int,
+                                    C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int, C.c_int,
+                                    C.c_int]
+    L.opiv_batch_destroy.argtypes = [C.c_void_p]
+    L.opiv_batch_frames.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)]
+    L.opiv_batch_upload.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t,
+                                    C.c_void_p]
+    L.opiv_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    L.opiv_batch_window_count.restype = C.c_int64
+    L.opiv_batch_window_count.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.opiv_batch_results.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -302,6 +317,58 @@ class MultiPass:
         disp = np.zeros(n, np.int32)
         _check(load().opiv_multipass_results(self._h, k, vec.ctypes.data, pk.ctypes.data,
                                              disp.ctypes.data))
+        return vec, pk, unpack_disp(disp)
+
+
+class Batch:
+    """Many image pairs (sizes may differ) through one multi-pass schedule,
+    submitted together (optionally as one replayed CUDA graph)."""
+
+    def __init__(self, sizes, dtype, passes, mode: int = CORR_COMPLEX,
+                 limit_search: bool = False, device: int = 0):
+        L = load()
+        self.dtype = np.dtype(dtype)
+        n = len(sizes)
+        ws = (C.c_uint32 * n)(*[s[0] for s in sizes])
+        hs = (C.c_uint32 * n)(*[s[1] for s in sizes])
+        ia = (C.c_uint32 * len(passes))(*[p[0] for p in passes])
+        st = (C.c_uint32 * len(passes))(*[p[1] for p in passes])
+        h = C.c_void_p()
+        _check(L.opiv_batch_create(C.byref(h), n, ws, hs, DTYPES[self.dtype], len(passes), ia, st,
+                                   mode, int(bool(limit_search)), device))
+        self._h = h
+        self.sizes, self.passes = list(sizes), list(passes)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().opiv_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, pair: int, frame_a: np.ndarray, frame_b: np.ndarray, stream: int = 0):
+        fa = np.ascontiguousarray(frame_a, self.dtype)
+        fb = np.ascontiguousarray(frame_b, self.dtype)
+        _check(load().opiv_batch_upload(self._h, pair, fa.ctypes.data, fb.ctypes.data,
+                                        fa.strides[0], stream or None))
+
+    def run(self, use_graph: bool = True, stream: int = 0):
+        _check(load().opiv_batch_run(self._h, int(bool(use_graph)), stream or None))
+
+    def window_count(self, pair: int, k: int) -> int:
+        return int(load().opiv_batch_window_count(self._h, pair, k))
+
+    def results(self, pair: int, k: int):
+        n = self.window_count(pair, k)
+        vec = np.zeros((n, 5), np.float32)
+        pk = np.zeros(n, np.int32)
+        disp = np.zeros(n, np.int32)
+        _check(load().opiv_batch_results(self._h, pair, k, vec.ctypes.data, pk.ctypes.data,
+                                         disp.ctypes.data))
         return vec, pk, unpack_disp(disp)
 
 

@@ -94,6 +94,44 @@ def config2(pair: int = 0, size: int = 4096):
                          seed=SEED_BASE + 1000 * 2 + pair, full_scale=4095.0)
 
 
+CONFIG3_SIZES = ((1024, 1024), (2048, 1536), (3072, 2048), (4096, 4096))   # (width, height)
+LAMB_OSEEN_ALPHA = 1.25643   # r = rc is the radius of maximum swirl velocity
+
+
+def lamb_oseen(cx: float, cy: float, rc: float = 150.0, vmax: float = 8.0,
+               offset: tuple[float, float] = (0.0, 0.0)):
+    """Lamb-Oseen vortex centred at (cx, cy): swirl velocity
+    v(r) = vmax (1 + 1/(2 alpha)) (rc / r) (1 - exp(-alpha r^2 / rc^2)), which
+    peaks at vmax for r = rc, plus a uniform offset."""
+    k = vmax * (1.0 + 0.5 / LAMB_OSEEN_ALPHA) * rc
+
+    def field(x, y):
+        dx, dy = x - cx, y - cy
+        r2 = dx * dx + dy * dy + 1e-12
+        s = k * (1.0 - np.exp(-LAMB_OSEEN_ALPHA * r2 / (rc * rc))) / r2
+        return -dy * s + offset[0], dx * s + offset[1]
+    return field
+
+
+def config3_layout(n_pairs: int = 48):
+    """Per pair: (width, height) drawn from CONFIG3_SIZES and the uniform
+    offset U(-2, 2)^2 px, by the config-3 seed."""
+    rng = np.random.Generator(np.random.PCG64(SEED_BASE + 1000 * 3))
+    idx = rng.integers(0, len(CONFIG3_SIZES), n_pairs)
+    off = rng.uniform(-2.0, 2.0, (n_pairs, 2))
+    return [(CONFIG3_SIZES[i], (float(o[0]), float(o[1]))) for i, o in zip(idx, off)]
+
+
+def config3(pair: int, size: tuple[int, int], offset: tuple[float, float]):
+    """One pair of the batched multi-pass workload: uint16 (12-bit signal) with
+    config-2 particle statistics, Lamb-Oseen vortex (core radius 150 px, peak
+    8 px) at the image centre plus the pair's uniform offset."""
+    w, h = size
+    return particle_pair(h, w, ppp=0.03, i0_range=(1500, 4000), noise=20.0,
+                         displacement=lamb_oseen(w / 2.0, h / 2.0, offset=offset),
+                         dtype=np.uint16, seed=SEED_BASE + 1000 * 3 + 1 + pair, full_scale=4095.0)
+
+
 def config5(pair: int = 0, size: int = 2048):
     """2048^2 float32 in [0, 1], ppp 0.02, I0 ~ U(0.6, 1), sigma 0.02, shift (0.40, 0.25)."""
     return particle_pair(size, size, ppp=0.02, i0_range=(0.6, 1.0), noise=0.02,

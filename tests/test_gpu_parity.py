@@ -295,3 +295,75 @@ def test_multipass_64_32_16_vs_oracle_chain(orc, mode):
         assert_vectors_match(vec, pk, ref[k]["vec"], ref[k]["peak"], ia, f"pass {k}")
         assert np.array_equal(disp, ref[k]["disp"]), f"pass {k}: integer displacements differ"
     mp.close()
+
+
+@pytest.mark.parametrize("mode", [og.CORR_POCKET, og.CORR_POCKET_REAL])
+def test_pocket_modes_are_the_circular_correlation(mode):
+    """PocketFFT::cross_correlate and ::cross_correlate_real (c2c and r2c/c2r
+    with fct 1.0) both give the true circular correlation: the same results
+    as the complex mode, whose planes match numpy's FFT correlation."""
+    a, b = synth.config1()
+    p1 = og.Plan(1024, 1024, np.uint8, 32, 16, mode=mode)
+    p2 = og.Plan(1024, 1024, np.uint8, 32, 16, mode=og.CORR_COMPLEX)
+    v1, k1 = p1.process(a, b)
+    v2, k2 = p2.process(a, b)
+    assert np.array_equal(v1, v2) and np.array_equal(k1, k2)
+    rng = np.random.default_rng(8)
+    wa = rng.integers(0, 256, (4, 32, 32)).astype(np.float64)
+    wb = rng.integers(0, 256, (4, 32, 32)).astype(np.float64)
+    got = og.cross_correlate_batch(wa, wb, mode)
+    ref = np.fft.fftshift(np.fft.ifft2(np.fft.fft2(wb) * np.conj(np.fft.fft2(wa))).real * 1024,
+                          axes=(1, 2))
+    for k in range(4):
+        assert np.abs(got[k] - ref[k]).max() <= PLANE_RTOL * np.abs(ref[k]).max()
+
+
+# ---- batches of image pairs -----------------------------------------------------
+def test_batch_graph_matches_per_pair_multipass():
+    """Pairs of different sizes through the 64/32/16 schedule as one batch:
+    eager submission, the first graph call (eager run + capture) and graph
+    replays after new frames are uploaded all give exactly the per-pair
+    MultiPass results."""
+    sizes = [(512, 384), (768, 512), (1024, 1024)]
+    passes = [(64, 32), (32, 16), (16, 8)]
+    frames = []
+    for i, (w, h) in enumerate(sizes):
+        for j in range(2):
+            frames.append(synth.particle_pair(
+                h, w, ppp=0.03, i0_range=(1500, 4000), noise=20.0,
+                displacement=synth.lamb_oseen(w / 2.0, h / 2.0, offset=(1.1 - i, 0.4 + j)),
+                dtype=np.uint16, seed=synth.SEED_BASE + 3900 + 10 * i + j, full_scale=4095.0))
+    expect = []
+    for i, (w, h) in enumerate(sizes):
+        per = []
+        for j in range(2):
+            mp = og.MultiPass(w, h, np.uint16, passes)
+            mp.process(*frames[2 * i + j])
+            per.append([mp.results(k) for k in range(len(passes))])
+            mp.close()
+        expect.append(per)
+    batch = og.Batch(sizes, np.uint16, passes)
+
+    def check(j, label):
+        for i in range(len(sizes)):
+            for k in range(len(passes)):
+                got = batch.results(i, k)
+                ref = expect[i][j][k]
+                for g, r, name in zip(got, ref, ("vectors", "peaks", "displacements")):
+                    assert np.array_equal(g, r), f"{label}: pair {i} pass {k} {name} differ"
+
+    for i in range(len(sizes)):
+        batch.upload(i, *frames[2 * i])
+    batch.run(use_graph=False)
+    check(0, "eager")
+    before = og.kernel_launch_count()
+    batch.run(use_graph=True)             # eager run + capture
+    check(0, "first graph call")
+    for j in (1, 0, 1):
+        for i in range(len(sizes)):
+            batch.upload(i, *frames[2 * i + j])
+        batch.run(use_graph=True)         # replay
+        check(j, f"replay {j}")
+    assert og.kernel_launch_count() - before == 4 * 2 * len(sizes) * len(passes)
+    assert batch.window_count(2, 2) == 127 * 127
+    batch.close()
