@@ -181,6 +181,29 @@ def cpu_baseline(a, b, grid, budget_s: float = 15.0):
                       f"complex mode, {threads} threads, {secs:.1f} s"}
 
 
+# executed tensor-core FLOPs per 32 x 32 window of the DFT-GEMM kernel: per
+# tile of 8 windows, 36 products of M = 128, N = 32, K = 16 (stage 1: 8,
+# stage 2: 16, stage 3: 8, stage 4: 4) per operand pass; split BF16 runs 3
+# passes (hi*hi, hi*lo, lo*hi)
+TC_FLOP_PER_WINDOW_PASS = 36 * 2 * 128 * 32 * 16 / 8
+
+
+def accuracy(vec, pk, ref_vec, ref_pk):
+    """Displacement error against the FP64 pass: RMS and max of (u, v) over
+    windows with the same integer peak, and the peak-mismatch rate."""
+    mask = 0xFFFF
+    a = np.where(pk >= 0, pk & mask, pk)
+    r = np.where(ref_pk >= 0, ref_pk & mask, ref_pk)
+    same = a == r
+    d = (vec[:, 2:4] - ref_vec[:, 2:4])[same]
+    ok = np.isfinite(d).all(1)
+    d = d[ok]
+    return {"rms_px": float(np.sqrt(np.mean(d ** 2))) if d.size else None,
+            "max_px": float(np.abs(d).max()) if d.size else None,
+            "peak_mismatch_rate": float(1.0 - same.mean()),
+            "nan_mismatch": int((~ok).sum())}
+
+
 def run_ours(args):
     import torch
 
@@ -191,103 +214,146 @@ def run_ours(args):
     dev = local
     torch.cuda.set_device(dev)
     a, b = synth.config2(pair=rank)
-    plan = og.Plan(IMG, IMG, np.uint16, IA, STEP, mode=og.CORR_COMPLEX, device=dev)
-    assert plan.n == N_WIN
-    plan.set_timing(True)
     stream = torch.cuda.Stream(device=dev)
     # resident copies of the pair at distinct addresses (defeats L2 reuse)
     frames = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)) for _ in range(L2_ROTATION)]
-    dvec = torch.empty((plan.n, 5), dtype=torch.float32, device=dev)
-    dpk = torch.empty(plan.n, dtype=torch.int32, device=dev)
     pitch = IMG * 2
-    launches0 = og.kernel_launch_count()
 
-    def step(k):
-        fa, fb = frames[k % L2_ROTATION]
-        plan.process_device(fa.data_ptr(), fb.data_ptr(), pitch, dvec.data_ptr(), dpk.data_ptr(),
-                            stream.cuda_stream)
+    def make_plan(precision):
+        plan = og.Plan(IMG, IMG, np.uint16, IA, STEP, mode=og.CORR_COMPLEX, device=dev)
+        assert plan.n == N_WIN
+        plan.set_precision(precision)
+        plan.set_timing(True)
+        return plan
+
+    def timed(plan, steps, warmup):
+        """Device-resident pass over the pair, `steps` times: (seconds over
+        all ranks, main-kernel ms per step, exact-pass ms per step,
+        launches, device outputs)."""
+        dvec = torch.empty((plan.n, 5), dtype=torch.float32, device=dev)
+        dpk = torch.empty(plan.n, dtype=torch.int32, device=dev)
+
+        def step(k):
+            fa, fb = frames[k % L2_ROTATION]
+            plan.process_device(fa.data_ptr(), fb.data_ptr(), pitch, dvec.data_ptr(),
+                                dpk.data_ptr(), stream.cuda_stream)
+
+        for k in range(warmup):
+            step(k)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        dist_barrier(world)
+        torch.cuda.synchronize()
+        launches_before = og.kernel_launch_count()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        main_ms, exact_ms = [], []
+        ev0.record(stream)
+        for k in range(steps):
+            step(k)
+            f, e = plan.last_timing()
+            main_ms.append(f)
+            exact_ms.append(e)
+        ev1.record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        dist_barrier(world)
+        elapsed = dist_max(ev0.elapsed_time(ev1) / 1e3, world)
+        plan.status()
+        return elapsed, main_ms, exact_ms, og.kernel_launch_count() - launches_before, dvec, dpk
 
     sampler = ClockSampler(dev)
     sampler.start()
-    for k in range(args.warmup):
-        step(k)
-    stream.synchronize()
-    torch.cuda.synchronize()
-    dist_barrier(world)
-    torch.cuda.synchronize()
-    launches_before = og.kernel_launch_count()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    fp32_ms, exact_ms, exact_windows = [], [], 0
-    ev0.record(stream)
-    for k in range(args.steps):
-        step(k)
-        f, e = plan.last_timing()
-        fp32_ms.append(f)
-        exact_ms.append(e)
-    ev1.record(stream)
-    stream.synchronize()
-    torch.cuda.synchronize()
-    dist_barrier(world)
-    elapsed = ev0.elapsed_time(ev1) / 1e3
-    elapsed = dist_max(elapsed, world)
-    gpu_launches = og.kernel_launch_count() - launches_before
-    exact_windows = plan.exact_count()
+    # ---- the tensor-core split-BF16 path (headline) and the plain FP32 path
+    tc_plan = make_plan(og.PREC_TC_SPLIT_BF16)
+    tc_el, tc_ms, _, tc_launches, tc_vec, tc_pk = timed(tc_plan, args.steps, args.warmup)
+    fp_plan = make_plan(og.PREC_FP32)
+    fp_el, fp_ms, ex_ms, fp_launches, fp_vec, fp_pk = timed(fp_plan, args.steps, args.warmup)
+    exact_windows = fp_plan.exact_count()
 
     # ---- end to end through the host-buffer call (pinned host memory)
     ha = torch.from_numpy(a).pin_memory()
     hb = torch.from_numpy(b).pin_memory()
-    hvec = torch.empty((plan.n, 5), dtype=torch.float32).pin_memory()
-    hpk = torch.empty(plan.n, dtype=torch.int32).pin_memory()
-    for _ in range(max(1, args.warmup)):
-        plan.process_into(ha.data_ptr(), hb.data_ptr(), pitch, hvec.data_ptr(), hpk.data_ptr())
-    dist_barrier(world)
-    e2e_steps = max(1, args.steps)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        plan.process_into(ha.data_ptr(), hb.data_ptr(), pitch, hvec.data_ptr(), hpk.data_ptr())
-    t_e2e = dist_max(time.perf_counter() - t0, world)
-    dist_barrier(world)
+    hvec = torch.empty((N_WIN, 5), dtype=torch.float32).pin_memory()
+    hpk = torch.empty(N_WIN, dtype=torch.int32).pin_memory()
+
+    def e2e(plan):
+        for _ in range(max(1, args.warmup)):
+            plan.process_into(ha.data_ptr(), hb.data_ptr(), pitch, hvec.data_ptr(), hpk.data_ptr())
+        dist_barrier(world)
+        n = max(1, args.steps)
+        t0 = time.perf_counter()
+        for _ in range(n):
+            plan.process_into(ha.data_ptr(), hb.data_ptr(), pitch, hvec.data_ptr(), hpk.data_ptr())
+        t = dist_max(time.perf_counter() - t0, world)
+        dist_barrier(world)
+        return n * N_WIN * world / t
+
+    fp_e2e = e2e(fp_plan)
+    assert torch.equal(fp_vec.cpu(), hvec), "device and host calls disagree (FP32 path)"
+    tc_e2e = e2e(tc_plan)
+    assert torch.equal(tc_vec.cpu(), hvec), "device and host calls disagree (tensor-core path)"
     clocks = sampler.stop()
 
-    # parity spot check of the timed output against the host call's output
-    assert torch.equal(dvec.cpu(), hvec), "device and host calls disagree"
+    # ---- accuracy against the FP64 pass (the reference's arithmetic on every window)
+    f64_plan = make_plan(og.PREC_FP64)
+    f64_vec, f64_pk = f64_plan.process(a, b)
+    bf_plan = make_plan(og.PREC_TC_BF16)
+    bf_el, _, _, _, bf_vec, bf_pk = timed(bf_plan, max(3, args.steps // 10), 3)
+    acc = {"tc_split_bf16": accuracy(tc_vec.cpu().numpy(), tc_pk.cpu().numpy(), f64_vec, f64_pk),
+           "tc_bf16": accuracy(bf_vec.cpu().numpy(), bf_pk.cpu().numpy(), f64_vec, f64_pk),
+           "fp32": accuracy(fp_vec.cpu().numpy(), fp_pk.cpu().numpy(), f64_vec, f64_pk)}
 
     if rank != 0:
         return
     peaks = peaks_file()
-    fp32_s = statistics.mean(fp32_ms) / 1e3
-    achieved = FLOP_PER_WINDOW * plan.n / fp32_s / 1e12
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-    value = args.steps * plan.n * world / elapsed
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    tc_s = statistics.mean(tc_ms) / 1e3
+    fp_s = statistics.mean(fp_ms) / 1e3
+    tc_flops = 3 * TC_FLOP_PER_WINDOW_PASS * N_WIN
+    achieved = tc_flops / tc_s / 1e12
+    value = args.steps * N_WIN * world / tc_el
+    plain_value = args.steps * N_WIN * world / fp_el
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "warmup": args.warmup, "ms_per_step": tc_el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3",
         "data": "synthetic (seeded particle images, 0.03 ppp, 12-bit)",
-        "config": {"workload": WORKLOAD, "windows_per_step": plan.n, "ia": IA, "step": STEP,
+        "config": {"workload": WORKLOAD, "windows_per_step": N_WIN, "ia": IA, "step": STEP,
                    "mode": "complex (FFT::cross_correlate)", "parallelism": f"replicas x{world}",
+                   "path": "tensor-core DFT-GEMM, split BF16 (hi*hi + hi*lo + lo*hi), FP32 accumulate",
                    "l2": f"{L2_ROTATION} resident copies of the pair rotated per step "
-                         f"({L2_ROTATION * 2 * IMG * IMG * 2 / 1e6:.0f} MB > 129 MB L2)",
-                   "exact_pass_windows_last_step": exact_windows},
-        "e2e": {"value": e2e_steps * plan.n * world / t_e2e, "unit": METRIC,
-                "h2d_bytes_per_step": 2 * IMG * IMG * 2,
-                "d2h_bytes_per_step": plan.n * (20 + 4)},
-        "gpu_launches": gpu_launches,
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
-                     "kernel": "piv_fp32_kernel<32,COMPLEX,u16>",
-                     "kernel_ms": statistics.mean(fp32_ms),
-                     "exact_pass_ms": statistics.mean(exact_ms),
-                     "peak_source": f"152 SMs x 128 FP32 lanes x 2 x {sm_max:.0f} MHz "
-                                    f"(sm_max_mhz of MEASURED_PEAKS.json)",
-                     "hbm_gbs_achieved": (2 * IMG * IMG * 2 + plan.n * 24) / fp32_s / 1e9,
+                         f"({L2_ROTATION * 2 * IMG * IMG * 2 / 1e6:.0f} MB > 129 MB L2)"},
+        "e2e": {"value": tc_e2e, "unit": METRIC, "h2d_bytes_per_step": 2 * IMG * IMG * 2,
+                "d2h_bytes_per_step": N_WIN * (20 + 4)},
+        "gpu_launches": tc_launches,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                     "frac": achieved / bf16_peak, "traffic": None,
+                     "kernel": "piv_tc_kernel<split,COMPLEX,u16>", "kernel_ms": statistics.mean(tc_ms),
+                     "flop": "executed MMA FLOPs: 3 passes x 36 products of 128x32x16 per 8 windows",
+                     "peak_source": "bf16_tflops of MEASURED_PEAKS.json (cuBLAS burst, of measured)",
+                     "hbm_gbs_achieved": (2 * IMG * IMG * 2 + N_WIN * 24) / tc_s / 1e9,
                      "hbm_gbs_peak": peaks.get("hbm_gbs")},
+        "accuracy_vs_fp64": acc,
+        "plain_fp32": {
+            "value": plain_value, "e2e": fp_e2e, "gpu_launches": fp_launches,
+            "ms_per_step": fp_el * 1e3 / args.steps,
+            "tc_speedup": value / plain_value,
+            "exact_pass_windows_last_step": exact_windows,
+            "roofline": {"bound": "fp32", "achieved": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12,
+                         "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12 / fp32_peak,
+                         "kernel": "piv_fp32_kernel<32,COMPLEX,u16>", "kernel_ms": statistics.mean(fp_ms),
+                         "exact_pass_ms": statistics.mean(ex_ms),
+                         "flop": "algorithmic: 2 x 5 N log2 N + 8 N, N = 1024, per window",
+                         "peak_source": f"152 SMs x 128 FP32 lanes x 2 x {sm_max:.0f} MHz"}},
+        "tc_bf16": {"value": max(3, args.steps // 10) * N_WIN * world / bf_el},
         "clocks": clocks,
     }
     if world == 1:
-        grid = plan.grid()
+        grid = fp_plan.grid()
         line["cpu_baseline"] = cpu_baseline(a, b, grid)
     print(json.dumps(line), flush=True)
 

@@ -41,7 +41,8 @@ enum {
     OPIV_ERR_SIZE_MISMATCH = -10, /* "image size is different from expected"    fft.h:94-98, :136-141 */
     OPIV_ERR_UNSUPPORTED = -11,   /* window size this build has no kernel for */
     OPIV_ERR_CUDA = -12,          /* a CUDA runtime call failed */
-    OPIV_ERR_NO_DEVICE = -13      /* no CUDA device */
+    OPIV_ERR_NO_DEVICE = -13,     /* no CUDA device */
+    OPIV_ERR_TIMEOUT = -14        /* a tensor-core kernel gave up waiting for its MMAs */
 };
 
 /* ---- enums -------------------------------------------------------------- */
@@ -129,6 +130,32 @@ int64_t opiv_plan_exact_count(opiv_plan* plan);
  * pass's durations in milliseconds. */
 int opiv_plan_set_timing(opiv_plan* plan, int enable);
 int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
+
+/* ---- precision of a plan's passes ---------------------------------------------
+ * No counterpart in the reference (it computes in double only).
+ * OPIV_PREC_FP32 (default): the FP32 kernels plus the exact re-decision
+ *   pass; integer peaks identical to the reference, u, v within 1e-4 px.
+ * OPIV_PREC_TC_SPLIT_BF16: 32 x 32 windows as four DFT matrix products on
+ *   the tensor cores, BF16 operands split into hi + lo parts, FP32
+ *   accumulation; no exact pass (a window whose top two plane values lie
+ *   within the rounding may pick the other peak).  Needs u8/u16 frames,
+ *   window x positions and x step multiples of 8 pixels, 16-byte aligned
+ *   rows; OPIV_ERR_UNSUPPORTED otherwise.
+ * OPIV_PREC_TC_BF16: the same with plain BF16 operands (one MMA per product).
+ * OPIV_PREC_FP64: every window through the exact FP64 kernel (the
+ *   reference's arithmetic, bit-identical planes): the oracle pass that the
+ *   other precisions are measured against.
+ * The last timing's "fp32_ms" is the main kernel of whichever precision. */
+enum { OPIV_PREC_FP32 = 0, OPIV_PREC_TC_SPLIT_BF16 = 1, OPIV_PREC_TC_BF16 = 2, OPIV_PREC_FP64 = 3 };
+int opiv_plan_set_precision(opiv_plan* plan, int precision);
+/* OPIV_OK, or OPIV_ERR_TIMEOUT if a tensor-core pass of this plan gave up
+ * waiting for its MMAs since the last call (waits for the plan's work). */
+int opiv_plan_status(opiv_plan* plan);
+/* Tensor-core precisions only: where the next passes also write every
+ * window's correlation plane after swap_quadrants, minus its pedestal
+ * sum(a) * sum(b) (n_win x 32 x 32 floats, device memory), and the
+ * pedestals (n_win doubles).  Null pointers switch the output off. */
+int opiv_plan_set_plane_output(opiv_plan* plan, float* d_planes, double* d_pedestals);
 
 /* ---- multi-pass window offsetting ------------------------------------------
  * No counterpart in the reference (its README lists multi-pass as to do,

@@ -102,6 +102,7 @@ std::vector<double2> reference_twiddles(uint32_t n, int dir)
 }
 
 constexpr int kExactBlocks = 152 * 2;   // CTAs of the exact pass (two per SM)
+constexpr int kExactAllBlocks = 152 * 8; // CTAs when every window takes the exact kernel
 
 // The PocketFFT modes compute the true circular correlation, as
 // FFT::cross_correlate does: they run the COMPLEX kernels.
@@ -142,6 +143,11 @@ struct opiv_plan {
     bool timing = false;
     cudaEvent_t ev[3] = { nullptr, nullptr, nullptr };   // fp32 start, fp32 end, exact end
     int32_t* d_disp = nullptr;          // integer displacements (multi-pass plans)
+    int precision = OPIV_PREC_FP32;
+    void* d_tc = nullptr;               // tensor-core constant matrices
+    int* d_status = nullptr;            // tensor-core wait status
+    float* d_planes = nullptr;          // optional plane output (tensor-core precisions)
+    double* d_peds = nullptr;
 };
 
 // A chain of plans over the same image pair: pass k's frame-B windows are
@@ -170,6 +176,8 @@ void plan_free(opiv_plan* p)
     cudaFree(p->d_flag_list);
     cudaFree(p->d_tw);
     cudaFree(p->d_disp);
+    cudaFree(p->d_tc);
+    cudaFree(p->d_status);
     if (p->h_flag_count) cudaFreeHost(p->h_flag_count);
     for (cudaEvent_t& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -221,6 +229,32 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.pw = (int)prev->ia;
     }
     CUDA_TRY(cudaMemsetAsync(p->d_flag_count, 0, sizeof(unsigned int), s));
+    if (p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_BF16) {
+        if (((uintptr_t)fa | (uintptr_t)fb | (uintptr_t)pitch) % 16 != 0)
+            return fail(OPIV_ERR_ARG, "the tensor-core path needs 16-byte aligned frame rows");
+        k.status = p->d_status;
+        k.planes = p->d_planes;
+        k.peds = p->d_peds;
+        if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
+        CUDA_TRY(launch_piv_tc(k, p->dtype, p->mode, p->limit,
+                               p->precision == OPIV_PREC_TC_SPLIT_BF16, p->d_tc, s));
+        ++g_launches;
+        if (p->timing) {
+            CUDA_TRY(cudaEventRecord(p->ev[1], s));
+            CUDA_TRY(cudaEventRecord(p->ev[2], s));
+        }
+        return OPIV_OK;
+    }
+    if (p->precision == OPIV_PREC_FP64) {
+        if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
+        CUDA_TRY(launch_piv_exact(k, (int)p->ia, p->dtype, p->mode, p->limit, false, kExactAllBlocks, s));
+        ++g_launches;
+        if (p->timing) {
+            CUDA_TRY(cudaEventRecord(p->ev[1], s));
+            CUDA_TRY(cudaEventRecord(p->ev[2], s));
+        }
+        return OPIV_OK;
+    }
     if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
     CUDA_TRY(launch_piv_fp32(k, (int)p->ia, p->dtype, p->mode, p->limit, false, s));
     ++g_launches;
@@ -254,6 +288,7 @@ const char* opiv_status_string(int s)
     case OPIV_ERR_UNSUPPORTED: return "unsupported window size";
     case OPIV_ERR_CUDA: return "CUDA error";
     case OPIV_ERR_NO_DEVICE: return "no CUDA device";
+    case OPIV_ERR_TIMEOUT: return "a tensor-core kernel gave up waiting for its MMAs";
     default: return "unknown status";
     }
 }
@@ -443,6 +478,7 @@ int opiv_process_pair(opiv_plan* plan, const void* frame_a, const void* frame_b,
                     cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
         return done(cuda_fail(e, "cudaStreamSynchronize"));
+    if (plan->d_status) return done(opiv_plan_status(plan));
     return done(OPIV_OK);
 }
 
@@ -777,6 +813,61 @@ int opiv_batch_results(opiv_batch* b, int pair, int pass, opiv_vector* out_vec, 
 {
     if (!b || pair < 0 || pair >= (int)b->pairs.size()) return fail(OPIV_ERR_ARG, "no such pair");
     return opiv_multipass_results(b->pairs[pair], pass, out_vec, out_peak, out_disp);
+}
+
+int opiv_plan_set_precision(opiv_plan* plan, int precision)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_FP64)
+        return fail(OPIV_ERR_ARG, "unknown precision %d", precision);
+    if (precision == OPIV_PREC_TC_SPLIT_BF16 || precision == OPIV_PREC_TC_BF16) {
+        if (!tc_supports((int)plan->ia, plan->dtype))
+            return fail(OPIV_ERR_UNSUPPORTED,
+                        "the tensor-core path takes 32x32 windows of u8/u16 frames");
+        if (plan->g.xs % 8 != 0 || plan->dx % 8 != 0)
+            return fail(OPIV_ERR_UNSUPPORTED,
+                        "the tensor-core path needs window x positions on multiples of 8 pixels");
+        if (!plan->d_tc) {
+            int prev = 0;
+            cudaGetDevice(&prev);
+            cudaSetDevice(plan->device);
+            std::vector<unsigned char> host(tc_constant_bytes());
+            tc_constants(host.data());
+            cudaError_t e = cudaMalloc(&plan->d_tc, host.size());
+            if (e == cudaSuccess)
+                e = cudaMemcpy(plan->d_tc, host.data(), host.size(), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMalloc(&plan->d_status, sizeof(int));
+            if (e == cudaSuccess) e = cudaMemset(plan->d_status, 0, sizeof(int));
+            cudaSetDevice(prev);
+            if (e != cudaSuccess) return cuda_fail(e, "tensor-core set-up");
+        }
+    }
+    plan->precision = precision;
+    return OPIV_OK;
+}
+
+int opiv_plan_status(opiv_plan* plan)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    if (!plan->d_status) return OPIV_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(plan->device);
+    int h = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && h) e = cudaMemset(plan->d_status, 0, sizeof(int));
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(e, "opiv_plan_status");
+    return h ? fail(OPIV_ERR_TIMEOUT, "a tensor-core pass gave up waiting for its MMAs") : OPIV_OK;
+}
+
+int opiv_plan_set_plane_output(opiv_plan* plan, float* d_planes, double* d_pedestals)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    plan->d_planes = d_planes;
+    plan->d_peds = d_pedestals;
+    return OPIV_OK;
 }
 
 int opiv_plan_set_timing(opiv_plan* plan, int enable)

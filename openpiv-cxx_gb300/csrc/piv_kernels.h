@@ -40,7 +40,18 @@ struct PivParams {
     const int32_t* prev_disp = nullptr;
     int pgx0 = 0, pgy0 = 0, pgdx = 1, pgdy = 1, pgnx = 1, pgny = 1, pw = 0;
     int32_t* out_disp = nullptr;       // this pass's integer displacements (may be null)
+    int* status = nullptr;             // tensor-core kernel: set to 1 if an MMA wait gave up
 };
+
+// Tensor-core DFT-GEMM kernel (piv_tc.cu): 32 x 32 windows, u8/u16 frames,
+// window x positions and steps multiples of 8 pixels.  Constant matrices,
+// each 32 x 32 BF16 hi + lo in the K-major no-swizzle operand layout.
+enum { kTcG1 = 0, kTcC = 1, kTcS = 2, kTcNS = 3, kTcC4 = 4, kTcNumMat = 5 };
+bool tc_supports(int w, int dtype);
+size_t tc_constant_bytes();
+void tc_constants(unsigned char* out);
+cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split,
+                          const void* consts, cudaStream_t s);
 
 // Fused FP32 kernels, one entry per window size (piv_fp32_w*.cu; 64 x 64
 // windows use the shared-memory kernel of piv_fp32_w64.cu).  Frames

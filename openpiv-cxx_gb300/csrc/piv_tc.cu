@@ -1,0 +1,654 @@
+// Tensor-core (tcgen05) PIV window path for 32 x 32 windows: the 2-D
+// cross-correlation of every window pair as four chained DFT matrix
+// products, BF16 operands split into hi + lo parts (hi*hi + hi*lo + lo*hi,
+// FP32 accumulation in tensor memory), then the reference's peak search,
+// 3-point Gaussian fit and vector (image_utils.impl.h:42-101,
+// main.cpp:214-236) on the CUDA cores.
+//
+// Mathematics (a, b: the two windows, rows y, columns x; all transforms
+// unnormalised like FFT::cross_correlate, fft.h:188-206):
+//   stage 1  row DFT of each window row as a real 32 x 32 product
+//            H = X * G: coefficients U_k = sum_x X cos(2 pi k x / 32)
+//            (k = 0..15), U_16 (coefficient (-1)^x), V_k = sum_x X sin(..)
+//            (k = 1..15); U_16 takes the slot of V_0, which is zero.
+//   stage 2  column DFT over y of the complex columns U_k - i V_k, as a
+//            real product with K = (U | V) x y; for the slot k = 0 this
+//            yields Z = DFT(U_0) - i DFT(U_16), unpacked by Hermitian
+//            symmetry.  The stored result is the conjugate spectrum.
+//   product  P = B conj(A) on the Hermitian half k_x = 0..16, the DC bin
+//            removed (its contribution sum(a) sum(b) is a constant, the
+//            pedestal, added back analytically in the fit), the k_y sign
+//            (-1)^k_y that swaps the plane's quadrants folded in, P(k_y, 0)
+//            and P(k_y, 16) packed as one complex column.
+//   stage 3  inverse column DFT over k_y (complex, real product K = (Re |
+//            Im) x k_y, N = (Re | Im) x y).
+//   stage 4  real inverse row DFT (c2r) over k_x, the weights 1 / 2 / 1 and
+//            the column quadrant swap folded into the constant matrix:
+//            the result is the swap_quadrants'ed plane minus its pedestal.
+//
+// One CTA of 4 warps runs tiles of 4 windows; warp w owns tensor-memory
+// lanes 32w .. 32w+31.  Every stage: CUDA cores write the operand into
+// shared memory (canonical no-swizzle layout, hi and lo parts), one thread
+// issues the MMAs and commits them to an mbarrier, all threads wait
+// (bounded) and read the accumulator back with tcgen05.ld.  Four CTAs
+// (54 KB of shared memory, 64 tensor-memory columns each) share an SM, so
+// the MMAs of some overlap the CUDA-core work of the others.
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "offsets.cuh"
+#include "piv_kernels.h"
+#include "tc_ptx.cuh"
+
+namespace opiv {
+namespace tc {
+
+constexpr int W = 32;
+constexpr int kThreads = 128;
+constexpr int kTile = 4;                        // windows per tile
+constexpr int kMat = 2048;                      // one 32 x 32 BF16 matrix, K-major
+constexpr int kConstBytes = kTcNumMat * 2 * kMat;
+constexpr int kDataBytes = 34 * 1024;
+constexpr int kTailBytes = 128;                 // pedestal sums, origins, mbarrier, TMEM slot, flag
+constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
+constexpr uint32_t kTmemCols = 64;
+constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
+constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (inside unused stage-3 rows)
+constexpr int kPRow = 36;                       // E4 plane row (floats), padded
+
+#define TC_NEG_INF (-__int_as_float(0x7f800000))
+
+// byte offset of element (n, k) in a 32 x 32 K-major matrix
+__host__ __device__ constexpr int kmaj32(int n, int k)
+{
+    return ((n >> 3) * 4 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2;
+}
+
+// hi / lo BF16 parts of 8 floats, packed for one 16-byte core-matrix row
+__device__ __forceinline__ void split8(const float* v, uint4& hi, uint4& lo)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const __nv_bfloat162 hb = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        const float2 hf = __bfloat1622float2(hb);
+        const __nv_bfloat162 lb = __floats2bfloat162_rn(v[2 * j] - hf.x, v[2 * j + 1] - hf.y);
+        h[j] = *reinterpret_cast<const uint32_t*>(&hb);
+        l[j] = *reinterpret_cast<const uint32_t*>(&lb);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// BF16 parts of 8 floats, hi only (single-pass precision)
+__device__ __forceinline__ uint4 round8(const float* v)
+{
+    uint32_t h[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const __nv_bfloat162 hb = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        h[j] = *reinterpret_cast<const uint32_t*>(&hb);
+    }
+    return make_uint4(h[0], h[1], h[2], h[3]);
+}
+
+template <bool SPLIT>
+__device__ __forceinline__ void put8(unsigned char* base, int off, const float* v)
+{
+    if (SPLIT) {
+        uint4 hi, lo;
+        split8(v, hi, lo);
+        *reinterpret_cast<uint4*>(base + off) = hi;
+        *reinterpret_cast<uint4*>(base + kLo + off) = lo;
+    } else {
+        *reinterpret_cast<uint4*>(base + off) = round8(v);
+    }
+}
+
+template <bool SPLIT>
+__device__ __forceinline__ void put1(unsigned char* base, int off, float v)
+{
+    const __nv_bfloat16 hb = __float2bfloat16_rn(v);
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = hb;
+    if (SPLIT) *reinterpret_cast<__nv_bfloat16*>(base + kLo + off) = __float2bfloat16_rn(v - __bfloat162float(hb));
+}
+
+// D (+)= A * B with hi/lo splitting: hi*hi, then hi*lo and lo*hi
+template <bool SPLIT>
+__device__ __forceinline__ void mma3(uint32_t d, uint32_t a_hi, uint32_t a_lbo, uint32_t a_sbo,
+                                     uint32_t b_hi, uint32_t b_lo, uint32_t idesc, bool acc)
+{
+    const uint64_t ah = tcx::sdesc(a_hi, a_lbo, a_sbo);
+    const uint64_t bh = tcx::sdesc(b_hi, 128, 512);
+    tcx::mma_bf16(d, ah, bh, idesc, acc);
+    if (SPLIT) {
+        tcx::mma_bf16(d, ah, tcx::sdesc(b_lo, 128, 512), idesc, true);
+        tcx::mma_bf16(d, tcx::sdesc(a_hi + kLo, a_lbo, a_sbo), bh, idesc, true);
+    }
+}
+
+template <typename PixT>
+__device__ __forceinline__ void load8(const PixT* ptr, float* px);
+
+template <>
+__device__ __forceinline__ void load8<uint16_t>(const uint16_t* ptr, float* px)
+{
+    const uint4 q = __ldg(reinterpret_cast<const uint4*>(ptr));
+    const uint32_t w[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        // exact widening: the 16-bit value in the low mantissa bits of 2^23
+        px[2 * j] = __uint_as_float(0x4b000000u | (w[j] & 0xffffu)) - 8388608.f;
+        px[2 * j + 1] = __uint_as_float(0x4b000000u | (w[j] >> 16)) - 8388608.f;
+    }
+}
+
+template <>
+__device__ __forceinline__ void load8<uint8_t>(const uint8_t* ptr, float* px)
+{
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(ptr));
+    const uint32_t w[2] = { q.x, q.y };
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        px[j] = __uint_as_float(0x4b000000u | ((w[0] >> (8 * j)) & 0xffu)) - 8388608.f;
+        px[4 + j] = __uint_as_float(0x4b000000u | ((w[1] >> (8 * j)) & 0xffu)) - 8388608.f;
+    }
+}
+
+template <bool SPLIT, int MODE, bool LIMIT, typename PixT>
+__global__ void __launch_bounds__(kThreads, 4)
+piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
+{
+    // peak scan range in swapped-plane coordinates (image_utils.impl.h:48,
+    // :54; limited search: rect::dilate(0.5), rect.cpp:109-126)
+    constexpr int D0 = LIMIT ? W / 4 : 0;
+    constexpr int VW = LIMIT ? W / 2 : W;
+    constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
+    constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
+    constexpr uint32_t kIdK32 = tcx::idesc_bf16(128, 32, false);
+    constexpr uint32_t kIdM32 = tcx::idesc_bf16(128, 32, true);
+
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char* cst = smem;
+    unsigned char* dat = smem + kConstBytes;
+    float* sums = reinterpret_cast<float*>(dat + kDataBytes);          // [window][frame]
+    int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // window corners
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(org + kTile);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t cst_a = tcx::smem_addr(cst), dat_a = tcx::smem_addr(dat);
+    auto mat = [&](int m, int lo) { return cst_a + (uint32_t)((2 * m + lo) * kMat); };
+
+    for (int i = tid; i < kConstBytes / 16; i += kThreads)
+        reinterpret_cast<uint4*>(cst)[i] = consts[i];
+    if (tid == 0) {
+        tcx::mbar_init(mbar, 1);
+        *abort_flag = 0;
+    }
+    if (warp == 0) tcx::tmem_alloc(tslot, kTmemCols);
+    tcx::fence_before();
+    __syncthreads();
+    tcx::fence_after();
+    const uint32_t tbase = *tslot;
+    const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
+
+    const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
+    const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
+    const size_t pitch = p.pitch / sizeof(PixT);
+    const int n_win = (int)p.n_win;
+    const int n_tiles = (n_win + kTile - 1) / kTile;
+    uint32_t phase = 0;
+
+    // wait for the committed MMAs; a wait that gives up aborts the CTA
+    auto wait_mma = [&]() {
+        if (!tcx::mbar_wait(mbar, phase)) {
+            *abort_flag = 1;
+            if (p.status) atomicExch(p.status, 1);
+        }
+        phase ^= 1u;
+        tcx::fence_after();
+    };
+
+    // item mapping of the pixel stage: 8 consecutive lanes fill one core
+    // matrix (rows R & 7), so the 16-byte stores are conflict-free
+    const int it_r7 = tid & 7, it_g = (tid >> 3) & 3, it_rg = tid >> 5;
+
+    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const int w0 = tile * kTile;
+        if (tid < kTile) {
+            const int gw = w0 + tid;
+            const int gy = (int)((unsigned)gw / (unsigned)p.gnx);
+            org[tid] = make_int2(p.gx0 + (gw - gy * p.gnx) * p.gdx, p.gy0 + gy * p.gdy);
+        }
+        __syncthreads();
+
+        // ---- stage-1 operand: window rows, K-major 256 x 32 (hi | lo);
+        // rows R = (2 m1 + wl) * 64 + f * 32 + y
+#pragma unroll 2
+        for (int t = 0; t < 8; ++t) {
+            const int R = (it_rg + 4 * t) * 8 + it_r7;
+            const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
+            float px[8];
+            if (w0 + w < n_win) {
+                const int2 o = org[w];
+                load8<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g, px);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j) px[j] = 0.f;
+            }
+            put8<SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
+        }
+        tcx::fence_proxy();
+        tcx::fence_before();
+        __syncthreads();
+        if (*abort_flag) break;
+
+        // ---- stage 1: H = X * G, two M-tiles of 128 rows
+        if (tid == 0) {
+            tcx::fence_after();
+#pragma unroll
+            for (int m1 = 0; m1 < 2; ++m1)
+#pragma unroll
+                for (int ks = 0; ks < 2; ++ks)
+                    mma3<SPLIT>(tbase + 32 * m1, dat_a + m1 * 8192 + ks * 256, 128, 512,
+                                mat(kTcG1, 0) + ks * 256, mat(kTcG1, 1) + ks * 256, kIdK32, ks > 0);
+            tcx::commit(mbar);
+        }
+        wait_mma();
+
+        // ---- E1: coefficients -> stage-2 operand (MN-major, rows
+        // (window, frame, k) = 128, K = (U | V) x y = 64); row sums
+#pragma unroll 1
+        for (int m1 = 0; m1 < 2; ++m1) {
+            float c[32];
+            tcx::tmem_ld32(tlane + 32 * m1, c);
+            const int w = 2 * m1 + (warp >> 1), f = warp & 1;
+            float s = c[0];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) sums[2 * w + f] = s;
+            const int g0 = (w * 32 + f * 16) >> 3;
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {
+                const int k = part * 32 + lane;
+                const int base = (k >> 3) * 2048 + (k & 7) * 16;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) put8<SPLIT>(dat, base + (g0 + h) * 128, c + part * 16 + h * 8);
+            }
+        }
+        tcx::fence_proxy();
+        tcx::fence_before();
+        __syncthreads();
+
+        // ---- stage 2: conj of the column DFT; N = 64 as two N = 32
+        // blocks: Re = U*C + V*(-S), -Im = U*S + V*C
+        if (tid == 0) {
+            tcx::fence_after();
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t a = dat_a + ks * 4096;
+                const int kk = ks & 1;
+                const int bre = ks < 2 ? kTcC : kTcNS, bim = ks < 2 ? kTcS : kTcC;
+                mma3<SPLIT>(tbase, a, 2048, 128, mat(bre, 0) + kk * 256, mat(bre, 1) + kk * 256,
+                            kIdM32, ks > 0);
+                mma3<SPLIT>(tbase + 32, a, 2048, 128, mat(bim, 0) + kk * 256, mat(bim, 1) + kk * 256,
+                            kIdM32, ks > 0);
+            }
+            tcx::commit(mbar);
+        }
+        wait_mma();
+
+        // ---- E2: products into the stage-3 operand (K-major, rows
+        // (window, k_x) = 64 of 128, K = (Re | Im) x k_y = 64).  Warp w holds
+        // window w: lane = frame * 16 + k_x.
+        {
+            const int w = warp;
+            const int f = lane >> 4, kxr = lane & 15;
+            float x[64];   // [k_y] = Re X, [32 + k_y] = -Im X of this lane's (frame, k_x)
+            tcx::tmem_ld32(tlane, x);
+            tcx::tmem_ld32(tlane + 32, x + 32);
+            // k_x slot 0 rows of both frames for the packed bins
+            float* pk = reinterpret_cast<float*>(dat + kPacked) + warp * 128;
+            if (kxr == 0) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    *reinterpret_cast<float4*>(pk + f * 64 + 4 * j) =
+                        make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
+            }
+            // frame a's lane computes k_y in [0, 16), frame b's in [16, 32):
+            // exchange halves with the partner lane (lane ^ 16)
+            float pr[16], pi[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float mr = f ? x[16 + j] : x[j], mn = f ? x[48 + j] : x[32 + j];
+                const float sr = f ? x[j] : x[16 + j], sn = f ? x[32 + j] : x[48 + j];
+                const float orr = __shfl_xor_sync(0xffffffffu, sr, 16);
+                const float onn = __shfl_xor_sync(0xffffffffu, sn, 16);
+                // A: frame a values, B: frame b values; n = -Im
+                const float ar = f ? orr : mr, an = f ? onn : mn;
+                const float br = f ? mr : orr, bn = f ? mn : onn;
+                // P = B conj(A), quadrant sign (-1)^k_y (parity of j)
+                float r = fmaf(br, ar, bn * an);
+                float q = fmaf(br, an, -(bn * ar));
+                if (j & 1) { r = -r; q = -q; }
+                if (MODE == kModeReal && j == 0) { r = 0.f; q = 0.f; }   // k_y = 0 or 16
+                pr[j] = r;
+                pi[j] = q;
+            }
+            if (kxr != 0) {
+                const int R3 = w * 16 + kxr;
+#pragma unroll
+                for (int part = 0; part < 2; ++part)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = part * 32 + 16 * f + 8 * h;
+                        put8<SPLIT>(dat, ((R3 >> 3) * 8 + (k >> 3)) * 128 + (R3 & 7) * 16,
+                                    (part ? pi : pr) + 8 * h);
+                    }
+            }
+            __syncwarp();
+            // packed row k_x = 0 | 16, one k_y per lane
+            {
+                const int ky = lane, kn = (32 - lane) & 31;
+                const float* sa = pk;          // frame a, k_x slot 0
+                const float* sb = pk + 64;     // frame b
+                // Z[k] = Re + i Im with Im = -stored
+                const float zar = sa[ky], zai = -sa[32 + ky], zanr = sa[kn], zani = -sa[32 + kn];
+                const float zbr = sb[ky], zbi = -sb[32 + ky], zbnr = sb[kn], zbni = -sb[32 + kn];
+                // X0 = (Z[k] + conj Z[-k]) / 2, X16 = i (Z[k] - conj Z[-k]) / 2
+                const float a0r = 0.5f * (zar + zanr), a0i = 0.5f * (zai - zani);
+                const float a6r = -0.5f * (zai + zani), a6i = 0.5f * (zar - zanr);
+                const float b0r = 0.5f * (zbr + zbnr), b0i = 0.5f * (zbi - zbni);
+                const float b6r = -0.5f * (zbi + zbni), b6i = 0.5f * (zbr - zbnr);
+                // P = B conj(A)
+                float p0r = b0r * a0r + b0i * a0i, p0i = b0i * a0r - b0r * a0i;
+                float p6r = b6r * a6r + b6i * a6i, p6i = b6i * a6r - b6r * a6i;
+                if (MODE == kModeReal) {
+                    p0r = 0.f; p0i = 0.f;
+                    if (ky == 0 || ky == 16) { p6r = 0.f; p6i = 0.f; }
+                } else if (ky == 0) {
+                    p0r = 0.f; p0i = 0.f;         // pedestal removed
+                }
+                // packed P(ky, 0) + i P(ky, 16), quadrant sign
+                float r = p0r - p6i, q = p0i + p6r;
+                if (ky & 1) { r = -r; q = -q; }
+                const int R0 = w * 16;
+                put1<SPLIT>(dat, ((R0 >> 3) * 8 + (ky >> 3)) * 128 + (ky & 7) * 2, r);
+                put1<SPLIT>(dat, ((R0 >> 3) * 8 + ((32 + ky) >> 3)) * 128 + (ky & 7) * 2, q);
+            }
+        }
+        tcx::fence_proxy();
+        tcx::fence_before();
+        __syncthreads();
+
+        // ---- stage 3: inverse column DFT, Re T = Pr*C + Pi*(-S),
+        // Im T = Pr*S + Pi*C (rows 64..127 of the M-tile are not used)
+        if (tid == 0) {
+            tcx::fence_after();
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+                const uint32_t a = dat_a + ks * 256;
+                const int kk = ks & 1;
+                const int bre = ks < 2 ? kTcC : kTcNS, bim = ks < 2 ? kTcS : kTcC;
+                mma3<SPLIT>(tbase, a, 128, 1024, mat(bre, 0) + kk * 256, mat(bre, 1) + kk * 256,
+                            kIdK32, ks > 0);
+                mma3<SPLIT>(tbase + 32, a, 128, 1024, mat(bim, 0) + kk * 256, mat(bim, 1) + kk * 256,
+                            kIdK32, ks > 0);
+            }
+            tcx::commit(mbar);
+        }
+        wait_mma();
+
+        // ---- E3: T into the stage-4 operand (MN-major, rows (window, y') =
+        // 128, K = (Re | Im) x k_x = 32); lanes 0..63 (warps 0, 1)
+        if (warp < 2) {
+            const int w = 2 * warp + (lane >> 4), kxr = lane & 15;
+            float t[32];
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {
+                tcx::tmem_ld32(tlane + 32 * part, t);
+                const int k = part * 16 + kxr;
+                const int base = (k >> 3) * 2048 + (k & 7) * 16;
+#pragma unroll
+                for (int g = 0; g < 4; ++g) put8<SPLIT>(dat, base + (w * 4 + g) * 128, t + 8 * g);
+            }
+        }
+        tcx::fence_proxy();
+        tcx::fence_before();
+        __syncthreads();
+
+        // ---- stage 4: real inverse row DFT, D = T * C4
+        if (tid == 0) {
+            tcx::fence_after();
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks)
+                mma3<SPLIT>(tbase, dat_a + ks * 4096, 2048, 128, mat(kTcC4, 0) + ks * 256,
+                            mat(kTcC4, 1) + ks * 256, kIdM32, ks > 0);
+            tcx::commit(mbar);
+        }
+        wait_mma();
+
+        // ---- E4: find_peaks(plane, 2, 1), fit, vector; warp w, row y' = lane
+        {
+            float* pl = reinterpret_cast<float*>(dat) + warp * (32 * kPRow);
+            const int w = warp;
+            const int gw = w0 + w;
+            const int y = lane;
+            float v[32];
+            tcx::tmem_ld32(tlane, v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<float4*>(pl + y * kPRow + 4 * j) =
+                    make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            __syncwarp();
+            float t0 = TC_NEG_INF, t1 = TC_NEG_INF;
+            int tx = 0;
+            if (y >= SY0 && y < SY1) {
+                const float* up = pl + (y - 1) * kPRow;
+                const float* dn = pl + (y + 1) * kPRow;
+#pragma unroll
+                for (int x4 = (SX0 & ~3); x4 < SX1; x4 += 4) {
+                    const float4 u4 = *reinterpret_cast<const float4*>(up + x4);
+                    const float4 d4 = *reinterpret_cast<const float4*>(dn + x4);
+                    const float uu[4] = { u4.x, u4.y, u4.z, u4.w }, dd[4] = { d4.x, d4.y, d4.z, d4.w };
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int x = x4 + e;
+                        if (x < SX0 || x >= SX1) continue;
+                        const float c = v[x];
+                        const float m = fmaxf(fmaxf(uu[e], dd[e]), fmaxf(v[x - 1], v[x + 1]));
+                        const float sv = (m < c) ? c : TC_NEG_INF;
+                        const bool gt = sv > t0;
+                        t1 = gt ? t0 : fmaxf(t1, sv);
+                        tx = gt ? x : tx;
+                        t0 = gt ? sv : t0;
+                    }
+                }
+            }
+            if (p.planes && gw < n_win) {
+#pragma unroll
+                for (int x = 0; x < W; ++x) p.planes[(size_t)gw * (W * W) + y * W + x] = v[x];
+            }
+            int key = y * W + tx;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float o0 = __shfl_xor_sync(0xffffffffu, t0, o);
+                const float o1 = __shfl_xor_sync(0xffffffffu, t1, o);
+                const int ok = __shfl_xor_sync(0xffffffffu, key, o);
+                const bool take = (o0 > t0) || (o0 == t0 && ok < key);
+                const float n1 = take ? fmaxf(t0, o1) : fmaxf(t1, o0);
+                t0 = take ? o0 : t0;
+                key = take ? ok : key;
+                t1 = n1;
+            }
+            // fit_simple_gaussian: six logarithms on six lanes, relative to
+            // the pedestal sum(a) sum(b)
+            const int px = key & (W - 1), py = key >> 5;
+            const float ped = sums[2 * w] * sums[2 * w + 1];
+            const int j = lane < 6 ? lane : 0;
+            // numerator / denominator positions of lane j's logarithm
+            const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
+            const int ny = (j == 3 || j == 4) ? py - 1 : (j == 5 ? py + 1 : py);
+            const int qx = (j == 0) ? px + 1 : px;
+            const int qy = (j == 3) ? py + 1 : py;
+            const float an = pl[(ny & 31) * kPRow + (nx & 31)];
+            const float ad = pl[(qy & 31) * kPRow + (qx & 31)];
+            const float lg = log1pf((an - ad) / (ad + ped));
+            const float lxr = __shfl_sync(0xffffffffu, lg, 0);
+            const float lxl = __shfl_sync(0xffffffffu, lg, 1);
+            const float lxrr = __shfl_sync(0xffffffffu, lg, 2);
+            const float lyd = __shfl_sync(0xffffffffu, lg, 3);
+            const float lyu = __shfl_sync(0xffffffffu, lg, 4);
+            const float lydd = __shfl_sync(0xffffffffu, lg, 5);
+            if (lane == 0 && gw < n_win) {
+                opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
+                int32_t code = -1;
+                const int2 o = org[w];
+                const bool has2 = t1 > TC_NEG_INF;
+                if (has2) {
+                    const float vc = pl[py * kPRow + px];
+                    const float C = vc + ped;
+                    const float L = pl[py * kPRow + px - 1] + ped, R = pl[py * kPRow + px + 1] + ped;
+                    const float U = pl[(py - 1) * kPRow + px] + ped, D = pl[(py + 1) * kPRow + px] + ped;
+                    const float nan = __int_as_float(0x7fffffff);
+                    const bool okx = L > 0.f && C > 0.f && R > 0.f;
+                    const bool oky = U > 0.f && C > 0.f && D > 0.f;
+                    const float fx = okx ? lxr / (2.f * (lxl + lxrr)) : nan;
+                    const float fy = oky ? lyd / (2.f * (lyu + lydd)) : nan;
+                    const float p0 = t0 + ped, p1 = t1 + ped;
+                    out.x = (float)(o.x + W / 2);
+                    out.y = (float)(p.img_h - (o.y + W / 2));
+                    out.u = (float)(W / 2 - px) - fx;
+                    out.v = (float)(W / 2 - py) - fy;
+                    out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
+                    code = key;
+                }
+                p.out_vec[gw] = out;
+                if (p.out_peak) p.out_peak[gw] = code;
+                if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
+                if (p.peds) p.peds[gw] = (double)sums[2 * w] * (double)sums[2 * w + 1];
+            }
+        }
+        tcx::fence_before();
+        __syncthreads();
+    }
+    tcx::fence_before();
+    __syncthreads();
+    tcx::fence_after();
+    if (warp == 0) tcx::tmem_dealloc(tbase, kTmemCols);
+}
+
+template <bool SPLIT, int MODE, bool LIMIT, typename PixT>
+cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
+{
+    auto kern = piv_tc_kernel<SPLIT, MODE, LIMIT, PixT>;
+    static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
+    static std::atomic<int> sm_count[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+        if (e != cudaSuccess) return e;
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        sm_count[dev & 63].store(sms);
+        attr_done.fetch_or(bit);
+    }
+    const int64_t tiles = (p.n_win + kTile - 1) / kTile;
+    const int64_t cap = 4 * (int64_t)sm_count[dev & 63].load();
+    const int blocks = (int)(tiles < cap ? tiles : cap);
+    if (blocks <= 0) return cudaSuccess;
+    kern<<<blocks, kThreads, kSmemBytes, s>>>(p, reinterpret_cast<const uint4*>(consts));
+    return cudaGetLastError();
+}
+
+template <bool SPLIT, int MODE, bool LIMIT>
+cudaError_t by_dtype(const PivParams& p, int dtype, const void* consts, cudaStream_t s)
+{
+    if (dtype == kU8) return launch_t<SPLIT, MODE, LIMIT, uint8_t>(p, consts, s);
+    return launch_t<SPLIT, MODE, LIMIT, uint16_t>(p, consts, s);
+}
+
+template <bool SPLIT>
+cudaError_t by_mode(const PivParams& p, int dtype, int mode, int limit, const void* consts,
+                    cudaStream_t s)
+{
+    if (mode == kModeReal)
+        return limit ? by_dtype<SPLIT, kModeReal, true>(p, dtype, consts, s)
+                     : by_dtype<SPLIT, kModeReal, false>(p, dtype, consts, s);
+    return limit ? by_dtype<SPLIT, kModeComplex, true>(p, dtype, consts, s)
+                 : by_dtype<SPLIT, kModeComplex, false>(p, dtype, consts, s);
+}
+
+// ---- host: the constant matrices ----------------------------------------------
+uint16_t bf16_bits(float f)
+{
+    // round to nearest even (finite inputs)
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    const uint32_t r = u + 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(r >> 16);
+}
+
+float bf16_value(uint16_t h)
+{
+    const uint32_t u = (uint32_t)h << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+}  // namespace tc
+
+bool tc_supports(int w, int dtype) { return w == 32 && (dtype == kU8 || dtype == kU16); }
+
+size_t tc_constant_bytes() { return (size_t)tc::kConstBytes; }
+
+void tc_constants(unsigned char* out)
+{
+    using namespace tc;
+    const double pi = 3.14159265358979323846;
+    auto put = [&](int m, int n, int k, double v) {
+        const uint16_t hi = bf16_bits((float)v);
+        const uint16_t lo = bf16_bits((float)(v - (double)bf16_value(hi)));
+        std::memcpy(out + (2 * m) * kMat + kmaj32(n, k), &hi, 2);
+        std::memcpy(out + (2 * m + 1) * kMat + kmaj32(n, k), &lo, 2);
+    };
+    for (int n = 0; n < 32; ++n)
+        for (int k = 0; k < 32; ++k) {
+            // stage 1, B[k = x][n = coefficient]
+            double g;
+            if (n < 16) g = std::cos(2 * pi * n * k / 32.0);
+            else if (n == 16) g = (k & 1) ? -1.0 : 1.0;
+            else g = std::sin(2 * pi * (n - 16) * k / 32.0);
+            put(kTcG1, n, k, g);
+            const double c = std::cos(2 * pi * n * k / 32.0), s = std::sin(2 * pi * n * k / 32.0);
+            put(kTcC, n, k, c);
+            put(kTcS, n, k, s);
+            put(kTcNS, n, k, -s);
+            // stage 4, B[k = (part, k_x)][n = x'], x = (x' + 16) mod 32
+            const int x = (n + 16) & 31;
+            const int part = k >> 4, kx = k & 15;
+            double v;
+            if (part == 0) v = kx == 0 ? 1.0 : 2.0 * std::cos(2 * pi * kx * x / 32.0);
+            else v = kx == 0 ? ((x & 1) ? -1.0 : 1.0) : -2.0 * std::sin(2 * pi * kx * x / 32.0);
+            put(kTcC4, n, k, v);
+        }
+}
+
+cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split,
+                          const void* consts, cudaStream_t s)
+{
+    return split ? tc::by_mode<true>(p, dtype, mode, limit, consts, s)
+                 : tc::by_mode<false>(p, dtype, mode, limit, consts, s);
+}
+
+}  // namespace opiv

@@ -37,6 +37,8 @@ ERR_SIZE_MISMATCH = -10
 ERR_UNSUPPORTED = -11
 ERR_CUDA = -12
 ERR_NO_DEVICE = -13
+ERR_TIMEOUT = -14
+PREC_FP32, PREC_TC_SPLIT_BF16, PREC_TC_BF16, PREC_FP64 = 0, 1, 2, 3
 
 DTYPES = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
 SYMBOLS = [
@@ -51,6 +53,7 @@ SYMBOLS = [
     "opiv_multipass_grid", "opiv_multipass_process", "opiv_multipass_process_device",
     "opiv_multipass_results", "opiv_batch_create", "opiv_batch_destroy", "opiv_batch_frames",
     "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
+    "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -103,6 +106,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_plan_exact_count.restype = C.c_int64
     L.opiv_plan_exact_count.argtypes = [C.c_void_p]
     L.opiv_plan_set_timing.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_status.argtypes = [C.c_void_p]
+    L.opiv_plan_set_plane_output.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.opiv_plan_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
     L.opiv_cross_correlate_batch.argtypes = [_dp, _dp, C.c_uint32, C.c_int64, C.c_int, C.c_int,
                                              _dp, C.c_int]
@@ -243,6 +249,18 @@ class Plan:
 
     def exact_count(self) -> int:
         return int(load().opiv_plan_exact_count(self._h))
+
+    def set_precision(self, precision: int):
+        """PREC_FP32 (default, reference-exact peaks), PREC_TC_SPLIT_BF16,
+        PREC_TC_BF16 (tensor cores, 32 x 32 windows) or PREC_FP64 (every
+        window through the exact kernel)."""
+        _check(load().opiv_plan_set_precision(self._h, precision))
+
+    def status(self):
+        _check(load().opiv_plan_status(self._h))
+
+    def set_plane_output(self, d_planes: int, d_pedestals: int):
+        _check(load().opiv_plan_set_plane_output(self._h, d_planes or None, d_pedestals or None))
 
     def set_timing(self, enable: bool = True):
         _check(load().opiv_plan_set_timing(self._h, int(bool(enable))))
