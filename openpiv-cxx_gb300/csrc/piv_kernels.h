@@ -45,8 +45,10 @@ struct PivParams {
 
 // Tensor-core DFT-GEMM kernel (piv_tc.cu): 32 x 32 windows, u8/u16 frames,
 // window x positions and steps multiples of 8 pixels.  Constant matrices,
-// each 32 x 32 BF16 hi + lo in the K-major no-swizzle operand layout.
-enum { kTcG1 = 0, kTcC = 1, kTcS = 2, kTcNS = 3, kTcC4 = 4, kTcNumMat = 5 };
+// each 32 x 32 BF16 in the K-major no-swizzle operand layout, all hi parts
+// then all lo parts; -S, C, S adjacent so that [C; S] and [-S; C] are
+// 64-row operands.
+enum { kTcG1 = 0, kTcNS = 1, kTcC = 2, kTcS = 3, kTcC4 = 4, kTcNumMat = 5 };
 bool tc_supports(int w, int dtype);
 size_t tc_constant_bytes();
 void tc_constants(unsigned char* out);

@@ -59,6 +59,8 @@ constexpr uint32_t kTmemCols = 64;
 constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
 constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (inside unused stage-3 rows)
 constexpr int kPRow = 36;                       // E4 plane row (floats), padded
+// One thread issues every MMA of a stage and commits them to the stage's
+// mbarrier.  The MMAs of the other CTAs on the SM overlap a CTA's waits.
 
 #define TC_NEG_INF (-__int_as_float(0x7f800000))
 
@@ -117,45 +119,64 @@ __device__ __forceinline__ void put1(unsigned char* base, int off, float v)
     if (SPLIT) *reinterpret_cast<__nv_bfloat16*>(base + kLo + off) = __float2bfloat16_rn(v - __bfloat162float(hb));
 }
 
-// D (+)= A * B with hi/lo splitting: hi*hi, then hi*lo and lo*hi
+// D (+)= A * B with hi/lo splitting: hi*hi, then hi*lo and lo*hi.  a and b
+// are descriptors of the hi parts; the start-address field counts 16-byte
+// units, so a byte offset o is added as o >> 4 (no carry: shared addresses
+// are below 2^18).
 template <bool SPLIT>
-__device__ __forceinline__ void mma3(uint32_t d, uint32_t a_hi, uint32_t a_lbo, uint32_t a_sbo,
-                                     uint32_t b_hi, uint32_t b_lo, uint32_t idesc, bool acc)
+__device__ __forceinline__ void mma3(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, bool acc)
 {
-    const uint64_t ah = tcx::sdesc(a_hi, a_lbo, a_sbo);
-    const uint64_t bh = tcx::sdesc(b_hi, 128, 512);
-    tcx::mma_bf16(d, ah, bh, idesc, acc);
+    tcx::mma_bf16(d, a, b, idesc, acc);
     if (SPLIT) {
-        tcx::mma_bf16(d, ah, tcx::sdesc(b_lo, 128, 512), idesc, true);
-        tcx::mma_bf16(d, tcx::sdesc(a_hi + kLo, a_lbo, a_sbo), bh, idesc, true);
+        tcx::mma_bf16(d, a, b + ((kTcNumMat * kMat) >> 4), idesc, true);
+        tcx::mma_bf16(d, a + (kLo >> 4), b, idesc, true);
     }
+}
+
+// 8 pixels of one window row: raw load, then exact widening to float (the
+// integer in the low mantissa bits of 2^23, minus 2^23)
+template <typename PixT> struct Raw;
+template <> struct Raw<uint16_t> {
+    using type = uint4;
+    __device__ static uint4 zero() { return make_uint4(0, 0, 0, 0); }
+};
+template <> struct Raw<uint8_t> {
+    using type = uint2;
+    __device__ static uint2 zero() { return make_uint2(0, 0); }
+};
+
+template <typename PixT>
+__device__ __forceinline__ typename Raw<PixT>::type load_raw(const PixT* ptr)
+{
+    return __ldg(reinterpret_cast<const typename Raw<PixT>::type*>(ptr));
 }
 
 template <typename PixT>
-__device__ __forceinline__ void load8(const PixT* ptr, float* px);
+__device__ __forceinline__ void widen8(const typename Raw<PixT>::type& q, float* px, float s);
 
+// s = +1 or -1: the pixels times s (one FMA each, like the subtraction)
 template <>
-__device__ __forceinline__ void load8<uint16_t>(const uint16_t* ptr, float* px)
+__device__ __forceinline__ void widen8<uint16_t>(const uint4& q, float* px, float s)
 {
-    const uint4 q = __ldg(reinterpret_cast<const uint4*>(ptr));
     const uint32_t w[4] = { q.x, q.y, q.z, q.w };
+    const float c = -8388608.f * s;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        // exact widening: the 16-bit value in the low mantissa bits of 2^23
-        px[2 * j] = __uint_as_float(0x4b000000u | (w[j] & 0xffffu)) - 8388608.f;
-        px[2 * j + 1] = __uint_as_float(0x4b000000u | (w[j] >> 16)) - 8388608.f;
+        // bytes {w.b0, w.b1, 0x00, 0x4b} and {w.b2, w.b3, 0x00, 0x4b}
+        px[2 * j] = fmaf(__uint_as_float(__byte_perm(w[j], 0x4b00u, 0x5410u)), s, c);
+        px[2 * j + 1] = fmaf(__uint_as_float(__byte_perm(w[j], 0x4b00u, 0x5432u)), s, c);
     }
 }
 
 template <>
-__device__ __forceinline__ void load8<uint8_t>(const uint8_t* ptr, float* px)
+__device__ __forceinline__ void widen8<uint8_t>(const uint2& q, float* px, float s)
 {
-    const uint2 q = __ldg(reinterpret_cast<const uint2*>(ptr));
     const uint32_t w[2] = { q.x, q.y };
+    const float c = -8388608.f * s;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        px[j] = __uint_as_float(0x4b000000u | ((w[0] >> (8 * j)) & 0xffu)) - 8388608.f;
-        px[4 + j] = __uint_as_float(0x4b000000u | ((w[1] >> (8 * j)) & 0xffu)) - 8388608.f;
+        px[j] = fmaf(__uint_as_float(__byte_perm(w[0], 0x4b00u, 0x5440u + j)), s, c);
+        px[4 + j] = fmaf(__uint_as_float(__byte_perm(w[1], 0x4b00u, 0x5440u + j)), s, c);
     }
 }
 
@@ -171,19 +192,28 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
     constexpr uint32_t kIdK32 = tcx::idesc_bf16(128, 32, false);
     constexpr uint32_t kIdM32 = tcx::idesc_bf16(128, 32, true);
+    constexpr uint32_t kIdK64 = tcx::idesc_bf16(128, 64, false);
+    constexpr uint32_t kIdM64 = tcx::idesc_bf16(128, 64, true);
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* cst = smem;
     unsigned char* dat = smem + kConstBytes;
     float* sums = reinterpret_cast<float*>(dat + kDataBytes);          // [window][frame]
     int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // window corners
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(org + kTile);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(org + 2 * kTile);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
     int* abort_flag = reinterpret_cast<int*>(tslot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t cst_a = tcx::smem_addr(cst), dat_a = tcx::smem_addr(dat);
-    auto mat = [&](int m, int lo) { return cst_a + (uint32_t)((2 * m + lo) * kMat); };
+    // descriptors: constant matrix m (hi part; the lo parts follow all hi
+    // parts), and the data buffer in the layouts of the four stages
+    const uint64_t dB = tcx::sdesc(cst_a, 128, 512);
+    auto mat = [&](int m, int ks) { return dB + (uint64_t)((m * kMat + ks * 256) >> 4); };
+    const uint64_t dA1 = tcx::sdesc(dat_a, 128, 512);     // K-major, 4 k-groups per row group
+    const uint64_t dA2 = tcx::sdesc(dat_a, 2048, 128);    // MN-major, k-group stride 2 KB
+    const uint64_t dA3 = tcx::sdesc(dat_a, 128, 1024);    // K-major, 8 k-groups per row group
+    auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
 
     for (int i = tid; i < kConstBytes / 16; i += kThreads)
         reinterpret_cast<uint4*>(cst)[i] = consts[i];
@@ -201,8 +231,15 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
     const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
     const size_t pitch = p.pitch / sizeof(PixT);
-    const int n_win = (int)p.n_win;
-    const int n_tiles = (n_win + kTile - 1) / kTile;
+    // tiles: kTile consecutive windows of one grid row; tile t is row
+    // t % gny of tile column t / gny, and each CTA walks a contiguous range
+    // of t, i.e. down a tile column: consecutive tiles share 24 of 32 rows
+    // (step 8), which the next tile then finds in L1
+    const int gny = (int)(p.n_win / p.gnx);
+    const int tpr = (p.gnx + kTile - 1) / kTile;
+    const int n_tiles = tpr * gny;
+    const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
+    const int t_end = (int)((int64_t)(blockIdx.x + 1) * n_tiles / gridDim.x);
     uint32_t phase = 0;
 
     // wait for the committed MMAs; a wait that gives up aborts the CTA
@@ -219,30 +256,41 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     // matrix (rows R & 7), so the 16-byte stores are conflict-free
     const int it_r7 = tid & 7, it_g = (tid >> 3) & 3, it_rg = tid >> 5;
 
-    for (int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const int w0 = tile * kTile;
-        if (tid < kTile) {
-            const int gw = w0 + tid;
-            const int gy = (int)((unsigned)gw / (unsigned)p.gnx);
-            org[tid] = make_int2(p.gx0 + (gw - gy * p.gnx) * p.gdx, p.gy0 + gy * p.gdy);
+    for (int tile = t_begin; tile < t_end; ++tile) {
+        const int tcol = tile / gny, trow = tile - tcol * gny;
+        const int w0 = trow * p.gnx + kTile * tcol;   // window index of slot 0
+        if (tid < 2 * kTile) {   // this tile's window corners, then the next tile's; x < 0: no window
+            const int t = tile + (tid >> 2), i = tid & (kTile - 1);
+            const int c = t / gny, r = t - c * gny, col = kTile * c + i;
+            org[tid] = (t < t_end && col < p.gnx) ? make_int2(p.gx0 + col * p.gdx, p.gy0 + r * p.gdy)
+                                                 : make_int2(-1, -1);
         }
         __syncthreads();
 
         // ---- stage-1 operand: window rows, K-major 256 x 32 (hi | lo);
-        // rows R = (2 m1 + wl) * 64 + f * 32 + y
-#pragma unroll 2
-        for (int t = 0; t < 8; ++t) {
-            const int R = (it_rg + 4 * t) * 8 + it_r7;
-            const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
-            float px[8];
-            if (w0 + w < n_win) {
-                const int2 o = org[w];
-                load8<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g, px);
-            } else {
+        // rows R = (2 m1 + wl) * 64 + f * 32 + y.  All eight loads are in
+        // flight before the first conversion.
+        {
+            typename Raw<PixT>::type raw[8];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) px[j] = 0.f;
+            for (int t = 0; t < 8; ++t) {
+                const int R = (it_rg + 4 * t) * 8 + it_r7;
+                const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
+                const int2 o = org[w];
+                raw[t] = (o.x >= 0)
+                             ? load_raw<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g)
+                             : Raw<PixT>::zero();
             }
-            put8<SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
+            // frame B rows times (-1)^y: its column spectrum comes out rotated
+            // by 16 in k_y (see E2); rows R have f = t & 1, y & 1 = R & 1
+            const float sb = (it_r7 & 1) ? -1.f : 1.f;
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int R = (it_rg + 4 * t) * 8 + it_r7;
+                float px[8];
+                widen8<PixT>(raw[t], px, (t & 1) ? sb : 1.f);
+                put8<SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
+            }
         }
         tcx::fence_proxy();
         tcx::fence_before();
@@ -256,20 +304,34 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             for (int m1 = 0; m1 < 2; ++m1)
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
-                    mma3<SPLIT>(tbase + 32 * m1, dat_a + m1 * 8192 + ks * 256, 128, 512,
-                                mat(kTcG1, 0) + ks * 256, mat(kTcG1, 1) + ks * 256, kIdK32, ks > 0);
+                    mma3<SPLIT>(tbase + 32 * m1, dA1 + off(m1 * 8192 + ks * 256), mat(kTcG1, ks),
+                                kIdK32, ks > 0);
             tcx::commit(mbar);
+        }
+        // the next tile's window rows into L2 while this tile computes
+        {
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int R = (it_rg + 4 * t) * 8 + it_r7;
+                const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
+                const int2 o = org[kTile + w];
+                if (o.x >= 0) {
+                    const PixT* q = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g;
+                    asm volatile("prefetch.global.L2 [%0];" :: "l"(q));
+                }
+            }
         }
         wait_mma();
 
         // ---- E1: coefficients -> stage-2 operand (MN-major, rows
         // (window, frame, k) = 128, K = (U | V) x y = 64); row sums
-#pragma unroll 1
+        float c2[64];
+        tcx::tmem_ld32x2(tlane, tlane + 32, c2, c2 + 32);
+#pragma unroll
         for (int m1 = 0; m1 < 2; ++m1) {
-            float c[32];
-            tcx::tmem_ld32(tlane + 32 * m1, c);
+            const float* c = c2 + 32 * m1;
             const int w = 2 * m1 + (warp >> 1), f = warp & 1;
-            float s = c[0];
+            float s = (f && (lane & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) sums[2 * w + f] = s;
@@ -286,20 +348,14 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_before();
         __syncthreads();
 
-        // ---- stage 2: conj of the column DFT; N = 64 as two N = 32
-        // blocks: Re = U*C + V*(-S), -Im = U*S + V*C
-        if (tid == 0) {
+        // ---- stage 2: conj of the column DFT: Re = U*C + V*(-S),
+        // -Im = U*S + V*C
+        if (tid == 0) {   // N = 64: the U part against [C; S], the V part against [-S; C]
             tcx::fence_after();
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-                const uint32_t a = dat_a + ks * 4096;
-                const int kk = ks & 1;
-                const int bre = ks < 2 ? kTcC : kTcNS, bim = ks < 2 ? kTcS : kTcC;
-                mma3<SPLIT>(tbase, a, 2048, 128, mat(bre, 0) + kk * 256, mat(bre, 1) + kk * 256,
-                            kIdM32, ks > 0);
-                mma3<SPLIT>(tbase + 32, a, 2048, 128, mat(bim, 0) + kk * 256, mat(bim, 1) + kk * 256,
-                            kIdM32, ks > 0);
-            }
+            for (int ks = 0; ks < 4; ++ks)
+                mma3<SPLIT>(tbase, dA2 + off(ks * 4096), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdM64,
+                            ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -311,8 +367,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             const int w = warp;
             const int f = lane >> 4, kxr = lane & 15;
             float x[64];   // [k_y] = Re X, [32 + k_y] = -Im X of this lane's (frame, k_x)
-            tcx::tmem_ld32(tlane, x);
-            tcx::tmem_ld32(tlane + 32, x + 32);
+            tcx::tmem_ld32x2(tlane, tlane + 32, x, x + 32);
             // k_x slot 0 rows of both frames for the packed bins
             float* pk = reinterpret_cast<float*>(dat + kPacked) + warp * 128;
             if (kxr == 0) {
@@ -321,22 +376,23 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                     *reinterpret_cast<float4*>(pk + f * 64 + 4 * j) =
                         make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
             }
-            // frame a's lane computes k_y in [0, 16), frame b's in [16, 32):
-            // exchange halves with the partner lane (lane ^ 16)
+            // frame a's lane computes k_y = j, frame b's k_y = 16 + j (j < 16).
+            // Frame b's columns are rotated by 16 (its rows were multiplied by
+            // (-1)^y), so both lanes find their own values at [j], [32 + j]
+            // and send their partner (lane ^ 16) the values at [16 + j],
+            // [48 + j].  With m = own, o = partner values and n = -Im:
+            // Re P = m_r o_r + m_n o_n, Im P = +-(o_r m_n - o_n m_r), the
+            // sign + for frame a (A = m) and - for frame b (A = o).
+            const float sq = f ? -1.f : 1.f;
             float pr[16], pi[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-                const float mr = f ? x[16 + j] : x[j], mn = f ? x[48 + j] : x[32 + j];
-                const float sr = f ? x[j] : x[16 + j], sn = f ? x[32 + j] : x[48 + j];
-                const float orr = __shfl_xor_sync(0xffffffffu, sr, 16);
-                const float onn = __shfl_xor_sync(0xffffffffu, sn, 16);
-                // A: frame a values, B: frame b values; n = -Im
-                const float ar = f ? orr : mr, an = f ? onn : mn;
-                const float br = f ? mr : orr, bn = f ? mn : onn;
-                // P = B conj(A), quadrant sign (-1)^k_y (parity of j)
-                float r = fmaf(br, ar, bn * an);
-                float q = fmaf(br, an, -(bn * ar));
-                if (j & 1) { r = -r; q = -q; }
+                const float mr = x[j], mn = x[32 + j];
+                const float orr = __shfl_xor_sync(0xffffffffu, x[16 + j], 16);
+                const float onn = __shfl_xor_sync(0xffffffffu, x[48 + j], 16);
+                float r = fmaf(mr, orr, mn * onn);
+                float q = sq * fmaf(orr, mn, -(onn * mr));
+                if (j & 1) { r = -r; q = -q; }   // quadrant sign (-1)^k_y
                 if (MODE == kModeReal && j == 0) { r = 0.f; q = 0.f; }   // k_y = 0 or 16
                 pr[j] = r;
                 pi[j] = q;
@@ -357,10 +413,11 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             {
                 const int ky = lane, kn = (32 - lane) & 31;
                 const float* sa = pk;          // frame a, k_x slot 0
-                const float* sb = pk + 64;     // frame b
+                const float* sb = pk + 64;     // frame b, columns rotated by 16
+                const int kb = (ky + 16) & 31, kbn = (kn + 16) & 31;
                 // Z[k] = Re + i Im with Im = -stored
                 const float zar = sa[ky], zai = -sa[32 + ky], zanr = sa[kn], zani = -sa[32 + kn];
-                const float zbr = sb[ky], zbi = -sb[32 + ky], zbnr = sb[kn], zbni = -sb[32 + kn];
+                const float zbr = sb[kb], zbi = -sb[32 + kb], zbnr = sb[kbn], zbni = -sb[32 + kbn];
                 // X0 = (Z[k] + conj Z[-k]) / 2, X16 = i (Z[k] - conj Z[-k]) / 2
                 const float a0r = 0.5f * (zar + zanr), a0i = 0.5f * (zai - zani);
                 const float a6r = -0.5f * (zai + zani), a6i = 0.5f * (zar - zanr);
@@ -389,18 +446,12 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 
         // ---- stage 3: inverse column DFT, Re T = Pr*C + Pi*(-S),
         // Im T = Pr*S + Pi*C (rows 64..127 of the M-tile are not used)
-        if (tid == 0) {
+        if (tid == 0) {   // N = 64: the Pr part against [C; S], the Pi part against [-S; C]
             tcx::fence_after();
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-                const uint32_t a = dat_a + ks * 256;
-                const int kk = ks & 1;
-                const int bre = ks < 2 ? kTcC : kTcNS, bim = ks < 2 ? kTcS : kTcC;
-                mma3<SPLIT>(tbase, a, 128, 1024, mat(bre, 0) + kk * 256, mat(bre, 1) + kk * 256,
-                            kIdK32, ks > 0);
-                mma3<SPLIT>(tbase + 32, a, 128, 1024, mat(bim, 0) + kk * 256, mat(bim, 1) + kk * 256,
-                            kIdK32, ks > 0);
-            }
+            for (int ks = 0; ks < 4; ++ks)
+                mma3<SPLIT>(tbase, dA3 + off(ks * 256), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdK64,
+                            ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -409,14 +460,14 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         // 128, K = (Re | Im) x k_x = 32); lanes 0..63 (warps 0, 1)
         if (warp < 2) {
             const int w = 2 * warp + (lane >> 4), kxr = lane & 15;
-            float t[32];
+            float t2[64];
+            tcx::tmem_ld32x2(tlane, tlane + 32, t2, t2 + 32);
 #pragma unroll
             for (int part = 0; part < 2; ++part) {
-                tcx::tmem_ld32(tlane + 32 * part, t);
                 const int k = part * 16 + kxr;
                 const int base = (k >> 3) * 2048 + (k & 7) * 16;
 #pragma unroll
-                for (int g = 0; g < 4; ++g) put8<SPLIT>(dat, base + (w * 4 + g) * 128, t + 8 * g);
+                for (int g = 0; g < 4; ++g) put8<SPLIT>(dat, base + (w * 4 + g) * 128, t2 + 32 * part + 8 * g);
             }
         }
         tcx::fence_proxy();
@@ -428,8 +479,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 2; ++ks)
-                mma3<SPLIT>(tbase, dat_a + ks * 4096, 2048, 128, mat(kTcC4, 0) + ks * 256,
-                            mat(kTcC4, 1) + ks * 256, kIdM32, ks > 0);
+                mma3<SPLIT>(tbase, dA2 + off(ks * 4096), mat(kTcC4, ks), kIdM32, ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -447,11 +497,15 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 *reinterpret_cast<float4*>(pl + y * kPRow + 4 * j) =
                     make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
             __syncwarp();
-            float t0 = TC_NEG_INF, t1 = TC_NEG_INF;
-            int tx = 0;
-            if (y >= SY0 && y < SY1) {
-                const float* up = pl + (y - 1) * kPRow;
-                const float* dn = pl + (y + 1) * kPRow;
+            // strict 4-neighbour maxima of this row, then the top two by a
+            // pairwise tree (ties: the lower column)
+            constexpr int NX = SX1 - SX0;
+            float T0[NX], T1[NX];
+            int I0[NX];
+            {
+                const int yy = (y >= SY0 && y < SY1) ? y : SY0;   // rows outside: masked below
+                const float* up = pl + (yy - 1) * kPRow;
+                const float* dn = pl + (yy + 1) * kPRow;
 #pragma unroll
                 for (int x4 = (SX0 & ~3); x4 < SX1; x4 += 4) {
                     const float4 u4 = *reinterpret_cast<const float4*>(up + x4);
@@ -463,15 +517,27 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                         if (x < SX0 || x >= SX1) continue;
                         const float c = v[x];
                         const float m = fmaxf(fmaxf(uu[e], dd[e]), fmaxf(v[x - 1], v[x + 1]));
-                        const float sv = (m < c) ? c : TC_NEG_INF;
-                        const bool gt = sv > t0;
-                        t1 = gt ? t0 : fmaxf(t1, sv);
-                        tx = gt ? x : tx;
-                        t0 = gt ? sv : t0;
+                        T0[x - SX0] = (m < c) ? c : TC_NEG_INF;
+                        T1[x - SX0] = TC_NEG_INF;
+                        I0[x - SX0] = x;
                     }
                 }
+#pragma unroll
+                for (int st = 1; st < NX; st *= 2)
+#pragma unroll
+                    for (int i = 0; i + st < NX; i += 2 * st) {
+                        const bool gt = T0[i + st] > T0[i];
+                        const float lo = fminf(T0[i], T0[i + st]);
+                        T1[i] = fmaxf(fmaxf(T1[i], T1[i + st]), lo);
+                        I0[i] = gt ? I0[i + st] : I0[i];
+                        T0[i] = gt ? T0[i + st] : T0[i];
+                    }
             }
-            if (p.planes && gw < n_win) {
+            const bool row_in = y >= SY0 && y < SY1;
+            float t0 = row_in ? T0[0] : TC_NEG_INF, t1 = row_in ? T1[0] : TC_NEG_INF;
+            const int tx = I0[0];
+            const bool valid = org[w].x >= 0;
+            if (p.planes && valid) {
 #pragma unroll
                 for (int x = 0; x < W; ++x) p.planes[(size_t)gw * (W * W) + y * W + x] = v[x];
             }
@@ -490,7 +556,9 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             // fit_simple_gaussian: six logarithms on six lanes, relative to
             // the pedestal sum(a) sum(b)
             const int px = key & (W - 1), py = key >> 5;
-            const float ped = sums[2 * w] * sums[2 * w + 1];
+            // REAL mode: the reference's unpack zeroes spectrum row 0, so its
+            // plane has no pedestal
+            const float ped = MODE == kModeReal ? 0.f : sums[2 * w] * sums[2 * w + 1];
             const int j = lane < 6 ? lane : 0;
             // numerator / denominator positions of lane j's logarithm
             const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
@@ -506,7 +574,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             const float lyd = __shfl_sync(0xffffffffu, lg, 3);
             const float lyu = __shfl_sync(0xffffffffu, lg, 4);
             const float lydd = __shfl_sync(0xffffffffu, lg, 5);
-            if (lane == 0 && gw < n_win) {
+            if (lane == 0 && valid) {
                 opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
                 int32_t code = -1;
                 const int2 o = org[w];
@@ -532,7 +600,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds) p.peds[gw] = (double)sums[2 * w] * (double)sums[2 * w + 1];
+                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sums[2 * w] * (double)sums[2 * w + 1];
             }
         }
         tcx::fence_before();
@@ -562,7 +630,7 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
         sm_count[dev & 63].store(sms);
         attr_done.fetch_or(bit);
     }
-    const int64_t tiles = (p.n_win + kTile - 1) / kTile;
+    const int64_t tiles = (int64_t)((p.gnx + kTile - 1) / kTile) * (p.n_win / p.gnx);
     const int64_t cap = 4 * (int64_t)sm_count[dev & 63].load();
     const int blocks = (int)(tiles < cap ? tiles : cap);
     if (blocks <= 0) return cudaSuccess;
@@ -619,8 +687,8 @@ void tc_constants(unsigned char* out)
     auto put = [&](int m, int n, int k, double v) {
         const uint16_t hi = bf16_bits((float)v);
         const uint16_t lo = bf16_bits((float)(v - (double)bf16_value(hi)));
-        std::memcpy(out + (2 * m) * kMat + kmaj32(n, k), &hi, 2);
-        std::memcpy(out + (2 * m + 1) * kMat + kmaj32(n, k), &lo, 2);
+        std::memcpy(out + m * kMat + kmaj32(n, k), &hi, 2);
+        std::memcpy(out + (kTcNumMat + m) * kMat + kmaj32(n, k), &lo, 2);
     };
     for (int n = 0; n < 32; ++n)
         for (int k = 0; k < 32; ++k) {
