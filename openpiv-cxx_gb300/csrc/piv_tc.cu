@@ -53,7 +53,7 @@ constexpr int kTile = 4;                        // windows per tile
 constexpr int kMat = 2048;                      // one 32 x 32 BF16 matrix, K-major
 constexpr int kConstBytes = kTcNumMat * 2 * kMat;
 constexpr int kDataBytes = 34 * 1024;
-constexpr int kTailBytes = 128;                 // pedestal sums, origins, mbarrier, TMEM slot, flag
+constexpr int kTailBytes = 768;                 // sums, origins, indices, row sums, mbarrier, TMEM slot, flag
 constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
 constexpr uint32_t kTmemCols = 64;
 constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
@@ -180,7 +180,11 @@ __device__ __forceinline__ void widen8<uint8_t>(const uint2& q, float* px, float
     }
 }
 
-template <bool SPLIT, int MODE, bool LIMIT, typename PixT>
+// VT: vertical tiles, four windows of one grid column (row step <= 8): their
+// rows overlap, so stage 1 transforms each image row once (56 rows per frame
+// instead of 4 x 32) and E1 copies its coefficients into every window that
+// contains the row.  Otherwise four windows of one grid row.
+template <bool SPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
 __global__ void __launch_bounds__(kThreads, 4)
 piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 {
@@ -200,7 +204,9 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     unsigned char* dat = smem + kConstBytes;
     float* sums = reinterpret_cast<float*>(dat + kDataBytes);          // [window][frame]
     int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // window corners
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(org + 2 * kTile);
+    int* gwi = reinterpret_cast<int*>(org + 2 * kTile);                 // window indices
+    float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);              // VT: row sums [frame][row]
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(rs + 128);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
     int* abort_flag = reinterpret_cast<int*>(tslot + 1);
 
@@ -231,13 +237,14 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
     const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
     const size_t pitch = p.pitch / sizeof(PixT);
-    // tiles: kTile consecutive windows of one grid row; tile t is row
-    // t % gny of tile column t / gny, and each CTA walks a contiguous range
-    // of t, i.e. down a tile column: consecutive tiles share 24 of 32 rows
-    // (step 8), which the next tile then finds in L1
+    // tiles: kTile consecutive windows of one grid column (VT) or row; each
+    // CTA walks a contiguous range of tiles down the grid, so consecutive
+    // tiles share image rows, which the next tile then finds in L1
     const int gny = (int)(p.n_win / p.gnx);
-    const int tpr = (p.gnx + kTile - 1) / kTile;
-    const int n_tiles = tpr * gny;
+    // tiles per walked line: a grid column of VT tiles, a grid row otherwise
+    const int n_line = VT ? p.gnx : gny;
+    const int per_line = VT ? (gny + kTile - 1) / kTile : (p.gnx + kTile - 1) / kTile;
+    const int n_tiles = n_line * per_line;
     const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
     const int t_end = (int)((int64_t)(blockIdx.x + 1) * n_tiles / gridDim.x);
     uint32_t phase = 0;
@@ -257,20 +264,52 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     const int it_r7 = tid & 7, it_g = (tid >> 3) & 3, it_rg = tid >> 5;
 
     for (int tile = t_begin; tile < t_end; ++tile) {
-        const int tcol = tile / gny, trow = tile - tcol * gny;
-        const int w0 = trow * p.gnx + kTile * tcol;   // window index of slot 0
-        if (tid < 2 * kTile) {   // this tile's window corners, then the next tile's; x < 0: no window
+        if (tid < 2 * kTile) {   // this tile's windows, then the next tile's; x < 0: no window
             const int t = tile + (tid >> 2), i = tid & (kTile - 1);
-            const int c = t / gny, r = t - c * gny, col = kTile * c + i;
-            org[tid] = (t < t_end && col < p.gnx) ? make_int2(p.gx0 + col * p.gdx, p.gy0 + r * p.gdy)
-                                                 : make_int2(-1, -1);
+            int col, row;
+            if (VT) {   // tile t: column t / per_line, rows kTile * (t % per_line) + i
+                const int c = t / per_line;
+                col = c;
+                row = kTile * (t - c * per_line) + i;
+            } else {    // tile t: row t % gny, columns kTile * (t / gny) + i
+                const int c = t / gny;
+                row = t - c * gny;
+                col = kTile * c + i;
+            }
+            const bool ok = t < t_end && col < p.gnx && row < gny;
+            org[tid] = ok ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy) : make_int2(-1, -1);
+            gwi[tid] = row * p.gnx + col;
         }
         __syncthreads();
 
+        // number of window rows of this tile (VT: image rows below its top)
+        const int vrows = VT ? (org[1].x >= 0 ? (org[2].x >= 0 ? (org[3].x >= 0 ? 3 : 2) : 1) : 0) * p.gdy + W
+                             : 0;
+        if constexpr (VT) {
+            // ---- stage-1 operand: rows R = f * 64 + y of the tile's image
+            // rows (y < vrows <= 56), K-major 128 x 32 (hi | lo)
+            const int2 o = org[0];
+            typename Raw<PixT>::type raw[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int R = (it_rg + 4 * t) * 8 + it_r7;
+                const int f = t >> 1, y = R & 63;
+                raw[t] = (o.x >= 0 && y < vrows)
+                             ? load_raw<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g)
+                             : Raw<PixT>::zero();
+            }
+            const float sb = (it_r7 & 1) ? -1.f : 1.f;   // frame B rows times (-1)^y
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int R = (it_rg + 4 * t) * 8 + it_r7;
+                float px[8];
+                widen8<PixT>(raw[t], px, (t >> 1) ? sb : 1.f);
+                put8<SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
+            }
+        } else {
         // ---- stage-1 operand: window rows, K-major 256 x 32 (hi | lo);
         // rows R = (2 m1 + wl) * 64 + f * 32 + y.  All eight loads are in
         // flight before the first conversion.
-        {
             typename Raw<PixT>::type raw[8];
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
@@ -297,11 +336,11 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         __syncthreads();
         if (*abort_flag) break;
 
-        // ---- stage 1: H = X * G, two M-tiles of 128 rows
+        // ---- stage 1: H = X * G, one (VT) or two M-tiles of 128 rows
         if (tid == 0) {
             tcx::fence_after();
 #pragma unroll
-            for (int m1 = 0; m1 < 2; ++m1)
+            for (int m1 = 0; m1 < (VT ? 1 : 2); ++m1)
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
                     mma3<SPLIT>(tbase + 32 * m1, dA1 + off(m1 * 8192 + ks * 256), mat(kTcG1, ks),
@@ -309,7 +348,18 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::commit(mbar);
         }
         // the next tile's window rows into L2 while this tile computes
-        {
+        if constexpr (VT) {
+            const int2 o = org[kTile];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int R = (it_rg + 4 * t) * 8 + it_r7;
+                const int f = t >> 1, y = R & 63;
+                if (o.x >= 0 && y < 56 && o.y + y < p.img_h) {
+                    const PixT* q = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g;
+                    asm volatile("prefetch.global.L2 [%0];" :: "l"(q));
+                }
+            }
+        } else {
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
                 const int R = (it_rg + 4 * t) * 8 + it_r7;
@@ -323,6 +373,40 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         wait_mma();
 
+        if constexpr (VT) {
+            // ---- E1: each image row's coefficients into every window that
+            // contains it (stage-2 operand, MN-major, rows (window, frame, k)
+            // = 128, K = (U | V) x window row = 64); row sums into rs
+            float c[32];
+            tcx::tmem_ld32(tlane, c);
+            const int f = warp >> 1, y = (warp & 1) * 32 + lane;
+            if (y < vrows) {
+                rs[f * 64 + y] = (f && (y & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
+                uint4 hi[4], lo[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (SPLIT) split8(c + 8 * q, hi[q], lo[q]);
+                    else hi[q] = round8(c + 8 * q);
+                }
+#pragma unroll
+                for (int i = 0; i < kTile; ++i) {
+                    const int yl = y - i * p.gdy;
+                    if (org[i].x >= 0 && yl >= 0 && yl < W) {
+                        const int g0 = (i * 32 + f * 16) >> 3;
+#pragma unroll
+                        for (int part = 0; part < 2; ++part) {
+                            const int k = part * 32 + yl;
+                            const int base = (k >> 3) * 2048 + (k & 7) * 16;
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                *reinterpret_cast<uint4*>(dat + base + (g0 + h) * 128) = hi[2 * part + h];
+                                if (SPLIT) *reinterpret_cast<uint4*>(dat + kLo + base + (g0 + h) * 128) = lo[2 * part + h];
+                            }
+                        }
+                    }
+                }
+            }
+        } else {
         // ---- E1: coefficients -> stage-2 operand (MN-major, rows
         // (window, frame, k) = 128, K = (U | V) x y = 64); row sums
         float c2[64];
@@ -344,9 +428,17 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 for (int h = 0; h < 2; ++h) put8<SPLIT>(dat, base + (g0 + h) * 128, c + part * 16 + h * 8);
             }
         }
+        }
         tcx::fence_proxy();
         tcx::fence_before();
         __syncthreads();
+        if (VT && tid >= 32 && tid < 32 + 2 * kTile) {   // window sums from the row sums
+            const int i = (tid - 32) >> 1, f = tid & 1;
+            float s = 0.f;
+            if (org[i].x >= 0)
+                for (int yl = 0; yl < W; ++yl) s += rs[f * 64 + i * p.gdy + yl];
+            sums[2 * i + f] = s;
+        }
 
         // ---- stage 2: conj of the column DFT: Re = U*C + V*(-S),
         // -Im = U*S + V*C
@@ -488,7 +580,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         {
             float* pl = reinterpret_cast<float*>(dat) + warp * (32 * kPRow);
             const int w = warp;
-            const int gw = w0 + w;
+            const int gw = gwi[w];
             const int y = lane;
             float v[32];
             tcx::tmem_ld32(tlane, v);
@@ -612,10 +704,10 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     if (warp == 0) tcx::tmem_dealloc(tbase, kTmemCols);
 }
 
-template <bool SPLIT, int MODE, bool LIMIT, typename PixT>
+template <bool SPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
 cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
 {
-    auto kern = piv_tc_kernel<SPLIT, MODE, LIMIT, PixT>;
+    auto kern = piv_tc_kernel<SPLIT, MODE, LIMIT, PixT, VT>;
     static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
     static std::atomic<int> sm_count[64];
     int dev = 0;
@@ -630,7 +722,9 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
         sm_count[dev & 63].store(sms);
         attr_done.fetch_or(bit);
     }
-    const int64_t tiles = (int64_t)((p.gnx + kTile - 1) / kTile) * (p.n_win / p.gnx);
+    const int64_t gny = p.n_win / p.gnx;
+    const int64_t tiles = VT ? (int64_t)p.gnx * ((gny + kTile - 1) / kTile)
+                             : gny * ((p.gnx + kTile - 1) / kTile);
     const int64_t cap = 4 * (int64_t)sm_count[dev & 63].load();
     const int blocks = (int)(tiles < cap ? tiles : cap);
     if (blocks <= 0) return cudaSuccess;
@@ -641,8 +735,12 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
 template <bool SPLIT, int MODE, bool LIMIT>
 cudaError_t by_dtype(const PivParams& p, int dtype, const void* consts, cudaStream_t s)
 {
-    if (dtype == kU8) return launch_t<SPLIT, MODE, LIMIT, uint8_t>(p, consts, s);
-    return launch_t<SPLIT, MODE, LIMIT, uint16_t>(p, consts, s);
+    const bool vt = p.gdy > 0 && p.gdy <= 8;   // four stacked windows span <= 56 rows
+    if (dtype == kU8)
+        return vt ? launch_t<SPLIT, MODE, LIMIT, uint8_t, true>(p, consts, s)
+                  : launch_t<SPLIT, MODE, LIMIT, uint8_t, false>(p, consts, s);
+    return vt ? launch_t<SPLIT, MODE, LIMIT, uint16_t, true>(p, consts, s)
+              : launch_t<SPLIT, MODE, LIMIT, uint16_t, false>(p, consts, s);
 }
 
 template <bool SPLIT>
