@@ -4,25 +4,35 @@
 Workload: one 4096 x 4096 uint16 image pair (12-bit particle images, seeded
 synthetic data), 32 x 32 interrogation windows at step 8 (75 % overlap):
 509 x 509 = 259,081 windows.  One step = one pass over the pair: every
-window extracted, FFT cross-correlated (reference default "complex" mode,
+window extracted, cross-correlated (reference default "complex" mode,
 FFT::cross_correlate), peak-searched, Gaussian-fitted, vector written.
 
-  value  vectors/s with the frames already in HBM (device-buffer C ABI call,
-         CUDA events on the launching stream); four resident copies of the
-         pair (268 MB > 129 MB L2) are rotated so that no step reads frames
-         another step left in L2;
+  value  vectors/s of the tensor-core split-BF16 path (DFT matrix products
+         on tcgen05, hi*hi + hi*lo + lo*hi, FP32 accumulation) with the
+         frames already in HBM (device-buffer C ABI call, CUDA events on the
+         launching stream); four resident copies of the pair (268 MB >
+         129 MB L2) are rotated so that no step reads frames another step
+         left in L2;
   e2e    the same through the host-buffer C ABI call opiv_process_pair:
          pinned host frames in, vectors (and peak codes) back in host
          memory, host-to-device and device-to-host copies inside the timed
          region;
-  roofline  the fused FP32 kernel: algorithmic FLOPs (2 complex 2-D FFTs of
-         5 N log2 N each + 8 N, N = 32*32, per window) per launch over its
-         CUDA-event duration, against the FP32 CUDA-core peak;
+  roofline  the tensor-core kernel: executed MMA FLOPs per launch over its
+         CUDA-event duration, against the measured BF16 tensor peak;
+  plain_fp32  the plain FP32 FFT path (reference-exact integer peaks):
+         vectors/s, e2e, and its kernel's algorithmic FLOPs (2 complex 2-D
+         FFTs of 5 N log2 N each + 8 N, N = 32*32, per window) against the
+         FP32 CUDA-core peak;
+  accuracy_vs_fp64  RMS / max displacement error and peak-mismatch rate of
+         each precision against the FP64 pass (every window through the
+         exact kernel: the reference's arithmetic);
   cpu_baseline  the reference's CPU path (the compiled reference where this
          host has it, else the oracle's restatement) on the host cores.
 
 `--impl reference` times the reference's own CPU implementation of the path
 (thread pool over all host cores) on the same workload instead.
+`--workload batch` times 48 pairs of mixed sizes through the 64/32/16 px
+multi-pass schedule (CUDA-graph replay).
 Multi-GPU: the path does not exchange data between windows; N ranks run N
 independent replicas (one pair each), value is the sum.
 """
@@ -181,11 +191,12 @@ def cpu_baseline(a, b, grid, budget_s: float = 15.0):
                       f"complex mode, {threads} threads, {secs:.1f} s"}
 
 
-# executed tensor-core FLOPs per 32 x 32 window of the DFT-GEMM kernel: per
-# tile of 8 windows, 36 products of M = 128, N = 32, K = 16 (stage 1: 8,
-# stage 2: 16, stage 3: 8, stage 4: 4) per operand pass; split BF16 runs 3
-# passes (hi*hi, hi*lo, lo*hi)
-TC_FLOP_PER_WINDOW_PASS = 36 * 2 * 128 * 32 * 16 / 8
+# executed tensor-core FLOPs per 32 x 32 window of the DFT-GEMM kernel
+# (vertical tiles of 4 windows): per tile and operand pass, products of
+# M = 128, K = 16 with N = 32 (stage 1: 2, stage 4: 2) and N = 64 (stages 2
+# and 3: 4 each), 2 M N K FLOPs each; split BF16 runs 3 passes (hi*hi,
+# hi*lo, lo*hi)
+TC_FLOP_PER_WINDOW_PASS = 2 * 128 * 16 * (2 * 32 + 4 * 64 + 4 * 64 + 2 * 32) / 4
 
 
 def accuracy(vec, pk, ref_vec, ref_pk):
@@ -332,7 +343,7 @@ def run_ours(args):
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": achieved / bf16_peak, "traffic": None,
                      "kernel": "piv_tc_kernel<split,COMPLEX,u16>", "kernel_ms": statistics.mean(tc_ms),
-                     "flop": "executed MMA FLOPs: 3 passes x 36 products of 128x32x16 per 8 windows",
+                     "flop": "executed MMA FLOPs: 3 passes x (4 N=32 + 8 N=64 products of M=128, K=16) per 4 windows",
                      "peak_source": "bf16_tflops of MEASURED_PEAKS.json (cuBLAS burst, of measured)",
                      "hbm_gbs_achieved": (2 * IMG * IMG * 2 + N_WIN * 24) / tc_s / 1e9,
                      "hbm_gbs_peak": peaks.get("hbm_gbs")},
