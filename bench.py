@@ -533,6 +533,51 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+# ---- precision sweep -----------------------------------------------------------
+def run_sweep(args):
+    """Displacement error of every precision against the FP64 pass on the
+    config-2 field: windows 16 / 32 / 64 px at 75 % overlap, at config-2
+    statistics, low seeding (0.005 ppp) and high noise (sigma 80).  The
+    tensor-core precisions cover 32 px windows; 48 px windows are not a
+    power of two, which the reference's FFT rejects (fft.h:76-84)."""
+    import torch
+
+    import opiv_gb300 as og
+    from opiv_gb300 import synth
+
+    torch.cuda.set_device(0)
+    size = args.sweep_size
+    precisions = [("fp32", og.PREC_FP32), ("tc_split_bf16", og.PREC_TC_SPLIT_BF16),
+                  ("tc_bf16", og.PREC_TC_BF16)]
+    rows = []
+    for variant in ("base", "sparse", "noisy"):
+        a, b = synth.config4(variant, size)
+        for ia in (16, 32, 64):
+            step = ia // 4
+
+            def plan(prec):
+                p = og.Plan(size, size, np.uint16, ia, step, mode=og.CORR_COMPLEX)
+                p.set_precision(prec)
+                return p
+
+            ref_vec, ref_pk = plan(og.PREC_FP64).process(a, b)
+            for name, prec in precisions:
+                if prec != og.PREC_FP32 and ia != 32:
+                    continue
+                p = plan(prec)
+                vec, pk = p.process(a, b)
+                p.set_timing(True)
+                for _ in range(3):
+                    vec, pk = p.process(a, b)
+                ms, _ = p.last_timing()
+                rows.append({"variant": variant, "ia": ia, "step": step, "precision": name,
+                             "windows": p.n, "kernel_ms": ms,
+                             **accuracy(vec, pk, ref_vec, ref_pk)})
+    print(json.dumps({"metric": "precision sweep vs FP64 pass", "size": size,
+                      "data": "synthetic config-2 field (seeded particle images, 12-bit)",
+                      "rows": rows}), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -579,9 +624,12 @@ def main():
                     help="timed steps (default 1000 for pair, 20 for batch)")
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pair", choices=["pair", "batch"],
+    ap.add_argument("--workload", default="pair", choices=["pair", "batch", "sweep"],
                     help="pair: one 4096^2 pair, 32 px windows at step 8 (default); "
-                         "batch: 48 pairs of mixed sizes through the 64/32/16 px schedule")
+                         "batch: 48 pairs of mixed sizes through the 64/32/16 px schedule; "
+                         "sweep: accuracy of every precision against the FP64 pass")
+    ap.add_argument("--sweep-size", type=int, default=2048,
+                    help="image size of the precision sweep")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 20 if args.workload == "batch" and args.impl == "ours" else 1000
@@ -590,6 +638,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "sweep":
+        run_sweep(args)
     else:
         run_ours(args)
 

@@ -132,6 +132,17 @@ def config3(pair: int, size: tuple[int, int], offset: tuple[float, float]):
                          dtype=np.uint16, seed=SEED_BASE + 1000 * 3 + 1 + pair, full_scale=4095.0)
 
 
+def config4(variant: str = "base", size: int = 4096):
+    """The config-2 field for the precision sweep: "base" (config-2
+    statistics), "sparse" (0.005 ppp) or "noisy" (sigma 80)."""
+    ppp = 0.005 if variant == "sparse" else 0.03
+    noise = 80.0 if variant == "noisy" else 20.0
+    k = {"base": 0, "sparse": 1, "noisy": 2}[variant]
+    return particle_pair(size, size, ppp=ppp, i0_range=(1500, 4000), noise=noise,
+                         displacement=config2_field, dtype=np.uint16,
+                         seed=SEED_BASE + 1000 * 4 + k, full_scale=4095.0)
+
+
 def config5(pair: int = 0, size: int = 2048):
     """2048^2 float32 in [0, 1], ppp 0.02, I0 ~ U(0.6, 1), sigma 0.02, shift (0.40, 0.25)."""
     return particle_pair(size, size, ppp=0.02, i0_range=(0.6, 1.0), noise=0.02,

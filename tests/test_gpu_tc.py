@@ -134,3 +134,16 @@ def test_precision_argument_errors():
     vec, _ = p.process(a, a)
     assert np.all(vec == 0)       # blank frames: no two peaks anywhere
     p.status()
+
+
+@pytest.mark.parametrize("variant", ["sparse", "noisy"])
+def test_precision_sweep_variants(variant):
+    """Low seeding (0.005 ppp) and high noise (sigma 80) on the config-2
+    field, 1024^2 crop: both tensor-core precisions inside the target."""
+    a, b = synth.config4(variant, size=1024)
+    ref = run(a, b, 8, og.PREC_FP64)
+    for precision, (rms_t, max_t, mm_t) in ((og.PREC_TC_SPLIT_BF16, (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH)),
+                                            (og.PREC_TC_BF16, (BF16_RMS, BF16_MAX, BF16_MISMATCH))):
+        got = run(a, b, 8, precision)
+        rms, mx, mm = displacement_error(got, ref)
+        assert rms <= rms_t and mx <= max_t and mm <= mm_t, (variant, precision, rms, mx, mm)
