@@ -123,6 +123,17 @@ int opiv_process_pair_device(opiv_plan* plan, const void* d_frame_a, const void*
  * re-evaluation (synchronises with the plan's last pass) */
 int64_t opiv_plan_exact_count(opiv_plan* plan);
 
+/* Many image pairs of the plan's size through opiv_process_pair's pass,
+ * pipelined: the upload of pair i+1 and the download of pair i-1 overlap
+ * the pass over pair i (two device slots, an upload and a download
+ * stream; frames in pinned host memory are needed for the overlap).  No
+ * counterpart in the reference (its loop handles one pair).  Returns when
+ * every pair's vectors (and peak codes if out_peak is not null) are in host
+ * memory. */
+int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* frames_a,
+                       const void* const* frames_b, size_t pitch_bytes, opiv_vector* const* out_vec,
+                       int32_t* const* out_peak);
+
 /* Kernel timing, the GPU counterpart of the reference's "processing time"
  * log (main.cpp:239, :304-309).  When enabled, every pass records CUDA
  * events around its two kernels on the pass's stream; opiv_plan_last_timing

@@ -148,6 +148,16 @@ struct opiv_plan {
     int* d_status = nullptr;            // tensor-core wait status
     float* d_planes = nullptr;          // optional plane output (tensor-core precisions)
     double* d_peds = nullptr;
+    // opiv_process_pairs: two slots of device frames and outputs, an upload
+    // and a download stream, and the events that order them with the passes
+    bool pipe = false;
+    cudaStream_t up = nullptr, down = nullptr;
+    void* p_fa[2] = { nullptr, nullptr };
+    void* p_fb[2] = { nullptr, nullptr };
+    opiv_vector* p_vec[2] = { nullptr, nullptr };
+    int32_t* p_peak[2] = { nullptr, nullptr };
+    cudaEvent_t ev_up[2] = { nullptr, nullptr }, ev_done[2] = { nullptr, nullptr },
+                ev_down[2] = { nullptr, nullptr };
 };
 
 // A chain of plans over the same image pair: pass k's frame-B windows are
@@ -178,6 +188,19 @@ void plan_free(opiv_plan* p)
     cudaFree(p->d_disp);
     cudaFree(p->d_tc);
     cudaFree(p->d_status);
+    if (p->up) cudaStreamSynchronize(p->up);
+    if (p->down) cudaStreamSynchronize(p->down);
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(p->p_fa[k]);
+        cudaFree(p->p_fb[k]);
+        cudaFree(p->p_vec[k]);
+        cudaFree(p->p_peak[k]);
+        if (p->ev_up[k]) cudaEventDestroy(p->ev_up[k]);
+        if (p->ev_done[k]) cudaEventDestroy(p->ev_done[k]);
+        if (p->ev_down[k]) cudaEventDestroy(p->ev_down[k]);
+    }
+    if (p->up) cudaStreamDestroy(p->up);
+    if (p->down) cudaStreamDestroy(p->down);
     if (p->h_flag_count) cudaFreeHost(p->h_flag_count);
     for (cudaEvent_t& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -477,6 +500,74 @@ int opiv_process_pair(opiv_plan* plan, const void* frame_a, const void* frame_b,
     cudaMemcpyAsync(plan->h_flag_count, plan->d_flag_count, sizeof(unsigned int),
                     cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return done(cuda_fail(e, "cudaStreamSynchronize"));
+    if (plan->d_status) return done(opiv_plan_status(plan));
+    return done(OPIV_OK);
+}
+
+int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* frames_a,
+                       const void* const* frames_b, size_t pitch_bytes, opiv_vector* const* out_vec,
+                       int32_t* const* out_peak)
+{
+    if (!plan || n_pairs < 0 || (n_pairs > 0 && (!frames_a || !frames_b || !out_vec)))
+        return fail(OPIV_ERR_ARG, "null argument");
+    if (n_pairs == 0) return OPIV_OK;
+    const size_t row = (size_t)plan->img_w * px_bytes(plan->dtype);
+    if (pitch_bytes < row) return fail(OPIV_ERR_ARG, "pitch %zu smaller than a row", pitch_bytes);
+    for (int64_t i = 0; i < n_pairs; ++i)
+        if (!frames_a[i] || !frames_b[i] || !out_vec[i] || (out_peak && !out_peak[i]))
+            return fail(OPIV_ERR_ARG, "null buffer for pair %lld", (long long)i);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(plan->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaError_t e = cudaSuccess;
+    if (!plan->pipe) {
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+            if ((e = cudaMalloc(&plan->p_fa[k], row * plan->img_h)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&plan->p_fb[k], row * plan->img_h)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&plan->p_vec[k], sizeof(opiv_vector) * plan->n_win)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&plan->p_peak[k], sizeof(int32_t) * plan->n_win)) != cudaSuccess) break;
+            if ((e = cudaEventCreateWithFlags(&plan->ev_up[k], cudaEventDisableTiming)) != cudaSuccess) break;
+            if ((e = cudaEventCreateWithFlags(&plan->ev_done[k], cudaEventDisableTiming)) != cudaSuccess) break;
+            e = cudaEventCreateWithFlags(&plan->ev_down[k], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->up, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->down, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return done(cuda_fail(e, "opiv_process_pairs set-up"));
+        plan->pipe = true;
+    }
+    // pair i uses slot k = i & 1: its upload waits until pass i-2 has read
+    // the slot's frames, its pass until the download of pair i-2 has read
+    // the slot's outputs; uploads, passes and downloads of neighbouring
+    // pairs overlap
+    cudaStream_t cs = plan->stream;
+    for (int64_t i = 0; i < n_pairs; ++i) {
+        const int k = (int)(i & 1);
+        if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(plan->up, plan->ev_done[k], 0));
+        if ((e = cudaMemcpy2DAsync(plan->p_fa[k], row, frames_a[i], pitch_bytes, row, plan->img_h,
+                                   cudaMemcpyHostToDevice, plan->up)) != cudaSuccess ||
+            (e = cudaMemcpy2DAsync(plan->p_fb[k], row, frames_b[i], pitch_bytes, row, plan->img_h,
+                                   cudaMemcpyHostToDevice, plan->up)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaMemcpy2DAsync(frames)"));
+        CUDA_TRY(cudaEventRecord(plan->ev_up[k], plan->up));
+        CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_up[k], 0));
+        if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_down[k], 0));
+        const int rc = run_pass(plan, plan->p_fa[k], plan->p_fb[k], row, plan->p_vec[k],
+                                out_peak ? plan->p_peak[k] : nullptr, cs);
+        if (rc != OPIV_OK) return done(rc);
+        CUDA_TRY(cudaEventRecord(plan->ev_done[k], cs));
+        CUDA_TRY(cudaStreamWaitEvent(plan->down, plan->ev_done[k], 0));
+        if ((e = cudaMemcpyAsync(out_vec[i], plan->p_vec[k], sizeof(opiv_vector) * plan->n_win,
+                                 cudaMemcpyDeviceToHost, plan->down)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaMemcpyAsync(vectors)"));
+        if (out_peak && (e = cudaMemcpyAsync(out_peak[i], plan->p_peak[k], sizeof(int32_t) * plan->n_win,
+                                             cudaMemcpyDeviceToHost, plan->down)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaMemcpyAsync(peaks)"));
+        CUDA_TRY(cudaEventRecord(plan->ev_down[k], plan->down));
+    }
+    if ((e = cudaStreamSynchronize(plan->down)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(cs)) != cudaSuccess)
         return done(cuda_fail(e, "cudaStreamSynchronize"));
     if (plan->d_status) return done(opiv_plan_status(plan));
     return done(OPIV_OK);

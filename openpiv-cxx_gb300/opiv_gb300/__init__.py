@@ -54,6 +54,7 @@ SYMBOLS = [
     "opiv_multipass_results", "opiv_batch_create", "opiv_batch_destroy", "opiv_batch_frames",
     "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
     "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
+    "opiv_process_pairs",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -107,6 +108,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_plan_exact_count.argtypes = [C.c_void_p]
     L.opiv_plan_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.opiv_plan_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_process_pairs.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p),
+                                     C.POINTER(C.c_void_p), C.c_size_t, C.POINTER(C.c_void_p),
+                                     C.POINTER(C.c_void_p)]
     L.opiv_plan_status.argtypes = [C.c_void_p]
     L.opiv_plan_set_plane_output.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.opiv_plan_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
@@ -249,6 +253,25 @@ class Plan:
 
     def exact_count(self) -> int:
         return int(load().opiv_plan_exact_count(self._h))
+
+    def process_pairs_into(self, ptrs_a, ptrs_b, pitch: int, ptrs_vec, ptrs_peak=None):
+        """Host pointers (pinned for overlap), one per pair: pipelined passes."""
+        n = len(ptrs_a)
+        arr = lambda xs: (C.c_void_p * n)(*xs)
+        _check(load().opiv_process_pairs(self._h, n, arr(ptrs_a), arr(ptrs_b), pitch, arr(ptrs_vec),
+                                         arr(ptrs_peak) if ptrs_peak is not None else None))
+
+    def process_pairs(self, pairs):
+        """[(frame_a, frame_b), ...] numpy frames -> [(vectors, peaks), ...]."""
+        fr = [(np.ascontiguousarray(a, self.dtype), np.ascontiguousarray(b, self.dtype)) for a, b in pairs]
+        for a, b in fr:
+            if a.shape != (self.img_h, self.img_w) or b.shape != (self.img_h, self.img_w):
+                raise OpivError(ERR_SIZE_MISMATCH, f"image size is different from expected: {a.shape}")
+        outs = [(np.zeros((self.n, 5), np.float32), np.zeros(self.n, np.int32)) for _ in fr]
+        self.process_pairs_into([a.ctypes.data for a, _ in fr], [b.ctypes.data for _, b in fr],
+                                fr[0][0].strides[0] if fr else 0,
+                                [v.ctypes.data for v, _ in outs], [p.ctypes.data for _, p in outs])
+        return outs
 
     def set_precision(self, precision: int):
         """PREC_FP32 (default, reference-exact peaks), PREC_TC_SPLIT_BF16,

@@ -367,3 +367,24 @@ def test_batch_graph_matches_per_pair_multipass():
     assert og.kernel_launch_count() - before == 4 * 2 * len(sizes) * len(passes)
     assert batch.window_count(2, 2) == 127 * 127
     batch.close()
+
+
+# ---- pipelined host call --------------------------------------------------------
+@pytest.mark.parametrize("precision", [og.PREC_FP32, og.PREC_TC_SPLIT_BF16])
+def test_process_pairs_equals_single_calls(precision):
+    """opiv_process_pairs (uploads, passes and downloads of neighbouring
+    pairs overlapped) gives exactly what one opiv_process_pair per pair
+    gives, in order."""
+    pairs = [synth.particle_pair(256, 384, ppp=0.03, i0_range=(1500, 4000), noise=20.0,
+                                 displacement=lambda x, y, s=s: (np.full_like(x, 0.7 * s), np.full_like(y, -1.1)),
+                                 dtype=np.uint16, seed=synth.SEED_BASE + 7000 + s, full_scale=4095.0)
+             for s in range(3)]
+    plan = og.Plan(384, 256, np.uint16, 32, 8)
+    plan.set_precision(precision)
+    single = [plan.process(a, b) for a, b in pairs]
+    seq = pairs + pairs[::-1]
+    got = plan.process_pairs(seq)
+    for (v, p), (rv, rp) in zip(got, single + single[::-1]):
+        assert np.array_equal(v.view(np.uint32), rv.view(np.uint32)) and np.array_equal(p, rp)
+    assert plan.process_pairs([]) == []
+    plan.close()
