@@ -57,7 +57,7 @@ constexpr int kTailBytes = 768;                 // sums, origins, indices, row s
 constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
 constexpr uint32_t kTmemCols = 64;
 constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
-constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (inside unused stage-3 rows)
+constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (after the stage-3 operand)
 constexpr int kPRow = 36;                       // E4 plane row (floats), padded
 // One thread issues every MMA of a stage and commits them to the stage's
 // mbarrier.  The MMAs of the other CTAs on the SM overlap a CTA's waits.
@@ -196,7 +196,9 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
     constexpr uint32_t kIdK32 = tcx::idesc_bf16(128, 32, false);
     constexpr uint32_t kIdM32 = tcx::idesc_bf16(128, 32, true);
-    constexpr uint32_t kIdK64 = tcx::idesc_bf16(128, 64, false);
+    // stage 3 has 64 rows: M = 64 puts row r in lane 32 (r / 16) + r % 16,
+    // i.e. window w's 16 rows in the first 16 lanes of warp w
+    constexpr uint32_t kIdK64M64 = tcx::idesc_bf16(64, 64, false);
     constexpr uint32_t kIdM64 = tcx::idesc_bf16(128, 64, true);
 
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -453,7 +455,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         wait_mma();
 
         // ---- E2: products into the stage-3 operand (K-major, rows
-        // (window, k_x) = 64 of 128, K = (Re | Im) x k_y = 64).  Warp w holds
+        // (window, k_x) = 64, K = (Re | Im) x k_y = 64).  Warp w holds
         // window w: lane = frame * 16 + k_x.
         {
             const int w = warp;
@@ -537,23 +539,24 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         __syncthreads();
 
         // ---- stage 3: inverse column DFT, Re T = Pr*C + Pi*(-S),
-        // Im T = Pr*S + Pi*C (rows 64..127 of the M-tile are not used)
+        // Im T = Pr*S + Pi*C (M = 64)
         if (tid == 0) {   // N = 64: the Pr part against [C; S], the Pi part against [-S; C]
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dA3 + off(ks * 256), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdK64,
+                mma3<SPLIT>(tbase, dA3 + off(ks * 256), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdK64M64,
                             ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
 
         // ---- E3: T into the stage-4 operand (MN-major, rows (window, y') =
-        // 128, K = (Re | Im) x k_x = 32); lanes 0..63 (warps 0, 1)
-        if (warp < 2) {
-            const int w = 2 * warp + (lane >> 4), kxr = lane & 15;
+        // 128, K = (Re | Im) x k_x = 32); warp w, lanes 0..15 = k_x
+        {
+            const int w = warp, kxr = lane;
             float t2[64];
             tcx::tmem_ld32x2(tlane, tlane + 32, t2, t2 + 32);
+            if (lane < 16)
 #pragma unroll
             for (int part = 0; part < 2; ++part) {
                 const int k = part * 16 + kxr;
@@ -584,35 +587,22 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             const int y = lane;
             float v[32];
             tcx::tmem_ld32(tlane, v);
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                *reinterpret_cast<float4*>(pl + y * kPRow + 4 * j) =
-                    make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-            __syncwarp();
-            // strict 4-neighbour maxima of this row, then the top two by a
-            // pairwise tree (ties: the lower column)
+            // strict 4-neighbour maxima of this row (rows above and below
+            // from the neighbouring lanes), then the top two by a pairwise
+            // tree (ties: the lower column)
             constexpr int NX = SX1 - SX0;
             float T0[NX], T1[NX];
             int I0[NX];
             {
-                const int yy = (y >= SY0 && y < SY1) ? y : SY0;   // rows outside: masked below
-                const float* up = pl + (yy - 1) * kPRow;
-                const float* dn = pl + (yy + 1) * kPRow;
 #pragma unroll
-                for (int x4 = (SX0 & ~3); x4 < SX1; x4 += 4) {
-                    const float4 u4 = *reinterpret_cast<const float4*>(up + x4);
-                    const float4 d4 = *reinterpret_cast<const float4*>(dn + x4);
-                    const float uu[4] = { u4.x, u4.y, u4.z, u4.w }, dd[4] = { d4.x, d4.y, d4.z, d4.w };
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int x = x4 + e;
-                        if (x < SX0 || x >= SX1) continue;
-                        const float c = v[x];
-                        const float m = fmaxf(fmaxf(uu[e], dd[e]), fmaxf(v[x - 1], v[x + 1]));
-                        T0[x - SX0] = (m < c) ? c : TC_NEG_INF;
-                        T1[x - SX0] = TC_NEG_INF;
-                        I0[x - SX0] = x;
-                    }
+                for (int x = SX0; x < SX1; ++x) {
+                    const float c = v[x];
+                    const float up = __shfl_up_sync(0xffffffffu, c, 1);
+                    const float dn = __shfl_down_sync(0xffffffffu, c, 1);
+                    const float m = fmaxf(fmaxf(up, dn), fmaxf(v[x - 1], v[x + 1]));
+                    T0[x - SX0] = (m < c) ? c : TC_NEG_INF;
+                    T1[x - SX0] = TC_NEG_INF;
+                    I0[x - SX0] = x;
                 }
 #pragma unroll
                 for (int st = 1; st < NX; st *= 2)
@@ -645,9 +635,17 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 key = take ? ok : key;
                 t1 = n1;
             }
-            // fit_simple_gaussian: six logarithms on six lanes, relative to
-            // the pedestal sum(a) sum(b)
+            // fit_simple_gaussian: the peak row and its neighbours into
+            // shared memory, six logarithms on six lanes, relative to the
+            // pedestal sum(a) sum(b)
             const int px = key & (W - 1), py = key >> 5;
+            if (y >= py - 1 && y <= py + 1) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    *reinterpret_cast<float4*>(pl + y * kPRow + 4 * j) =
+                        make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+            __syncwarp();
             // REAL mode: the reference's unpack zeroes spectrum row 0, so its
             // plane has no pedestal
             const float ped = MODE == kModeReal ? 0.f : sums[2 * w] * sums[2 * w + 1];
