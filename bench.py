@@ -321,11 +321,17 @@ def run_ours(args):
     # ---- accuracy against the FP64 pass (the reference's arithmetic on every window)
     f64_plan = make_plan(og.PREC_FP64)
     f64_vec, f64_pk = f64_plan.process(a, b)
-    bf_plan = make_plan(og.PREC_TC_BF16)
-    bf_el, _, _, _, bf_vec, bf_pk = timed(bf_plan, max(3, args.steps // 10), 3)
     acc = {"tc_split_bf16": accuracy(tc_vec.cpu().numpy(), tc_pk.cpu().numpy(), f64_vec, f64_pk),
-           "tc_bf16": accuracy(bf_vec.cpu().numpy(), bf_pk.cpu().numpy(), f64_vec, f64_pk),
            "fp32": accuracy(fp_vec.cpu().numpy(), fp_pk.cpu().numpy(), f64_vec, f64_pk)}
+    # the other tensor-core precisions: throughput (a shorter run) and accuracy
+    others = {}
+    for name, prec in (("tc_bf16", og.PREC_TC_BF16), ("tc_split_fp16", og.PREC_TC_SPLIT_FP16),
+                       ("tc_fp16", og.PREC_TC_FP16)):
+        pl = make_plan(prec)
+        n_o = max(3, args.steps // 10)
+        el, ms, _, _, v, k = timed(pl, n_o, 3)
+        others[name] = {"value": n_o * N_WIN * world / el, "kernel_ms": statistics.mean(ms)}
+        acc[name] = accuracy(v.cpu().numpy(), k.cpu().numpy(), f64_vec, f64_pk)
 
     if rank != 0:
         return
@@ -373,7 +379,7 @@ def run_ours(args):
                          "exact_pass_ms": statistics.mean(ex_ms),
                          "flop": "algorithmic: 2 x 5 N log2 N + 8 N, N = 1024, per window",
                          "peak_source": f"152 SMs x 128 FP32 lanes x 2 x {sm_max:.0f} MHz"}},
-        "tc_bf16": {"value": max(3, args.steps // 10) * N_WIN * world / bf_el},
+        "other_precisions": others,
         "clocks": clocks,
     }
     if world == 1:
@@ -561,7 +567,8 @@ def run_sweep(args):
     torch.cuda.set_device(0)
     size = args.sweep_size
     precisions = [("fp32", og.PREC_FP32), ("tc_split_bf16", og.PREC_TC_SPLIT_BF16),
-                  ("tc_bf16", og.PREC_TC_BF16)]
+                  ("tc_bf16", og.PREC_TC_BF16), ("tc_split_fp16", og.PREC_TC_SPLIT_FP16),
+                  ("tc_fp16", og.PREC_TC_FP16)]
     rows = []
     for variant in ("base", "sparse", "noisy"):
         a, b = synth.config4(variant, size)

@@ -153,11 +153,21 @@ int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
  *   window x positions and x step multiples of 8 pixels, 16-byte aligned
  *   rows; OPIV_ERR_UNSUPPORTED otherwise.
  * OPIV_PREC_TC_BF16: the same with plain BF16 operands (one MMA per product).
+ * OPIV_PREC_TC_SPLIT_FP16 / OPIV_PREC_TC_FP16: the same with FP16 operands
+ *   (11-bit significand), kept inside FP16's range by powers of two (a
+ *   fixed one per stage, one per window for the product), undone exactly.
  * OPIV_PREC_FP64: every window through the exact FP64 kernel (the
  *   reference's arithmetic, bit-identical planes): the oracle pass that the
  *   other precisions are measured against.
  * The last timing's "fp32_ms" is the main kernel of whichever precision. */
-enum { OPIV_PREC_FP32 = 0, OPIV_PREC_TC_SPLIT_BF16 = 1, OPIV_PREC_TC_BF16 = 2, OPIV_PREC_FP64 = 3 };
+enum {
+    OPIV_PREC_FP32 = 0,
+    OPIV_PREC_TC_SPLIT_BF16 = 1,
+    OPIV_PREC_TC_BF16 = 2,
+    OPIV_PREC_FP64 = 3,
+    OPIV_PREC_TC_SPLIT_FP16 = 4,
+    OPIV_PREC_TC_FP16 = 5
+};
 int opiv_plan_set_precision(opiv_plan* plan, int precision);
 /* OPIV_OK, or OPIV_ERR_TIMEOUT if a tensor-core pass of this plan gave up
  * waiting for its MMAs since the last call (waits for the plan's work). */

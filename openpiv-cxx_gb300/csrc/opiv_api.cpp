@@ -104,6 +104,12 @@ std::vector<double2> reference_twiddles(uint32_t n, int dir)
 constexpr int kExactBlocks = 152 * 2;   // CTAs of the exact pass (two per SM)
 constexpr int kExactAllBlocks = 152 * 8; // CTAs when every window takes the exact kernel
 
+bool is_tc(int precision)
+{
+    return precision == OPIV_PREC_TC_SPLIT_BF16 || precision == OPIV_PREC_TC_BF16 ||
+           precision == OPIV_PREC_TC_SPLIT_FP16 || precision == OPIV_PREC_TC_FP16;
+}
+
 // The PocketFFT modes compute the true circular correlation, as
 // FFT::cross_correlate does: they run the COMPLEX kernels.
 int kernel_mode(int mode)
@@ -252,7 +258,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.pw = (int)prev->ia;
     }
     CUDA_TRY(cudaMemsetAsync(p->d_flag_count, 0, sizeof(unsigned int), s));
-    if (p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_BF16) {
+    if (is_tc(p->precision)) {
         if (((uintptr_t)fa | (uintptr_t)fb | (uintptr_t)pitch) % 16 != 0)
             return fail(OPIV_ERR_ARG, "the tensor-core path needs 16-byte aligned frame rows");
         k.status = p->d_status;
@@ -260,7 +266,9 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.peds = p->d_peds;
         if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
         CUDA_TRY(launch_piv_tc(k, p->dtype, p->mode, p->limit,
-                               p->precision == OPIV_PREC_TC_SPLIT_BF16, p->d_tc, s));
+                               p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_SPLIT_FP16,
+                               p->precision == OPIV_PREC_TC_SPLIT_FP16 || p->precision == OPIV_PREC_TC_FP16,
+                               p->d_tc, s));
         ++g_launches;
         if (p->timing) {
             CUDA_TRY(cudaEventRecord(p->ev[1], s));
@@ -909,9 +917,9 @@ int opiv_batch_results(opiv_batch* b, int pair, int pass, opiv_vector* out_vec, 
 int opiv_plan_set_precision(opiv_plan* plan, int precision)
 {
     if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
-    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_FP64)
+    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_FP16)
         return fail(OPIV_ERR_ARG, "unknown precision %d", precision);
-    if (precision == OPIV_PREC_TC_SPLIT_BF16 || precision == OPIV_PREC_TC_BF16) {
+    if (is_tc(precision)) {
         if (!tc_supports((int)plan->ia, plan->dtype))
             return fail(OPIV_ERR_UNSUPPORTED,
                         "the tensor-core path takes 32x32 windows of u8/u16 frames");

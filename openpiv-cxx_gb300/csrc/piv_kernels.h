@@ -52,7 +52,8 @@ enum { kTcG1 = 0, kTcNS = 1, kTcC = 2, kTcS = 3, kTcC4 = 4, kTcNumMat = 5 };
 bool tc_supports(int w, int dtype);
 size_t tc_constant_bytes();
 void tc_constants(unsigned char* out);
-cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split,
+// consts: tc_constant_bytes() bytes from tc_constants (BF16 set, FP16 set)
+cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
                           const void* consts, cudaStream_t s);
 
 // Fused FP32 kernels, one entry per window size (piv_fp32_w*.cu; 64 x 64

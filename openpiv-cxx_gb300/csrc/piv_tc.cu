@@ -1,761 +1,34 @@
-// Tensor-core (tcgen05) PIV window path for 32 x 32 windows: the 2-D
-// cross-correlation of every window pair as four chained DFT matrix
-// products, BF16 operands split into hi + lo parts (hi*hi + hi*lo + lo*hi,
-// FP32 accumulation in tensor memory), then the reference's peak search,
-// 3-point Gaussian fit and vector (image_utils.impl.h:42-101,
-// main.cpp:214-236) on the CUDA cores.
-//
-// Mathematics (a, b: the two windows, rows y, columns x; all transforms
-// unnormalised like FFT::cross_correlate, fft.h:188-206):
-//   stage 1  row DFT of each window row as a real 32 x 32 product
-//            H = X * G: coefficients U_k = sum_x X cos(2 pi k x / 32)
-//            (k = 0..15), U_16 (coefficient (-1)^x), V_k = sum_x X sin(..)
-//            (k = 1..15); U_16 takes the slot of V_0, which is zero.
-//   stage 2  column DFT over y of the complex columns U_k - i V_k, as a
-//            real product with K = (U | V) x y; for the slot k = 0 this
-//            yields Z = DFT(U_0) - i DFT(U_16), unpacked by Hermitian
-//            symmetry.  The stored result is the conjugate spectrum.
-//   product  P = B conj(A) on the Hermitian half k_x = 0..16, the DC bin
-//            removed (its contribution sum(a) sum(b) is a constant, the
-//            pedestal, added back analytically in the fit), the k_y sign
-//            (-1)^k_y that swaps the plane's quadrants folded in, P(k_y, 0)
-//            and P(k_y, 16) packed as one complex column.
-//   stage 3  inverse column DFT over k_y (complex, real product K = (Re |
-//            Im) x k_y, N = (Re | Im) x y).
-//   stage 4  real inverse row DFT (c2r) over k_x, the weights 1 / 2 / 1 and
-//            the column quadrant swap folded into the constant matrix:
-//            the result is the swap_quadrants'ed plane minus its pedestal.
-//
-// One CTA of 4 warps runs tiles of 4 windows; warp w owns tensor-memory
-// lanes 32w .. 32w+31.  Every stage: CUDA cores write the operand into
-// shared memory (canonical no-swizzle layout, hi and lo parts), one thread
-// issues the MMAs and commits them to an mbarrier, all threads wait
-// (bounded) and read the accumulator back with tcgen05.ld.  Four CTAs
-// (54 KB of shared memory, 64 tensor-memory columns each) share an SM, so
-// the MMAs of some overlap the CUDA-core work of the others.
-#include <atomic>
+// Host side of the tensor-core kernel (piv_tc_kernel.cuh): the constant
+// matrices in BF16 and FP16 (hi and lo parts, canonical operand layout) and
+// the dispatch to the two instantiation units.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
-#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
-#include "offsets.cuh"
 #include "piv_kernels.h"
-#include "tc_ptx.cuh"
 
 namespace opiv {
+
+cudaError_t launch_piv_tc_bf16(const PivParams& p, int dtype, int mode, int limit, bool split,
+                               const void* consts, cudaStream_t s);
+cudaError_t launch_piv_tc_fp16(const PivParams& p, int dtype, int mode, int limit, bool split,
+                               const void* consts, cudaStream_t s);
+
 namespace tc {
 
-constexpr int W = 32;
-constexpr int kThreads = 128;
-constexpr int kTile = 4;                        // windows per tile
-constexpr int kMat = 2048;                      // one 32 x 32 BF16 matrix, K-major
-constexpr int kConstBytes = kTcNumMat * 2 * kMat;
-constexpr int kDataBytes = 34 * 1024;
-constexpr int kTailBytes = 768;                 // sums, origins, indices, row sums, mbarrier, TMEM slot, flag
-constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
-constexpr uint32_t kTmemCols = 64;
-constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
-constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (after the stage-3 operand)
-constexpr int kPRow = 36;                       // E4 plane row (floats), padded
-// One thread issues every MMA of a stage and commits them to the stage's
-// mbarrier.  The MMAs of the other CTAs on the SM overlap a CTA's waits.
-
-#define TC_NEG_INF (-__int_as_float(0x7f800000))
+constexpr int kMat = 2048;   // one 32 x 32 16-bit matrix
+constexpr int kSetBytes = kTcNumMat * 2 * kMat;
 
 // byte offset of element (n, k) in a 32 x 32 K-major matrix
-__host__ __device__ constexpr int kmaj32(int n, int k)
+constexpr int kmaj32(int n, int k)
 {
     return ((n >> 3) * 4 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2;
 }
 
-// hi / lo BF16 parts of 8 floats, packed for one 16-byte core-matrix row
-__device__ __forceinline__ void split8(const float* v, uint4& hi, uint4& lo)
-{
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const __nv_bfloat162 hb = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-        const float2 hf = __bfloat1622float2(hb);
-        const __nv_bfloat162 lb = __floats2bfloat162_rn(v[2 * j] - hf.x, v[2 * j + 1] - hf.y);
-        h[j] = *reinterpret_cast<const uint32_t*>(&hb);
-        l[j] = *reinterpret_cast<const uint32_t*>(&lb);
-    }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
-
-// BF16 parts of 8 floats, hi only (single-pass precision)
-__device__ __forceinline__ uint4 round8(const float* v)
-{
-    uint32_t h[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const __nv_bfloat162 hb = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-        h[j] = *reinterpret_cast<const uint32_t*>(&hb);
-    }
-    return make_uint4(h[0], h[1], h[2], h[3]);
-}
-
-template <bool SPLIT>
-__device__ __forceinline__ void put8(unsigned char* base, int off, const float* v)
-{
-    if (SPLIT) {
-        uint4 hi, lo;
-        split8(v, hi, lo);
-        *reinterpret_cast<uint4*>(base + off) = hi;
-        *reinterpret_cast<uint4*>(base + kLo + off) = lo;
-    } else {
-        *reinterpret_cast<uint4*>(base + off) = round8(v);
-    }
-}
-
-template <bool SPLIT>
-__device__ __forceinline__ void put1(unsigned char* base, int off, float v)
-{
-    const __nv_bfloat16 hb = __float2bfloat16_rn(v);
-    *reinterpret_cast<__nv_bfloat16*>(base + off) = hb;
-    if (SPLIT) *reinterpret_cast<__nv_bfloat16*>(base + kLo + off) = __float2bfloat16_rn(v - __bfloat162float(hb));
-}
-
-// D (+)= A * B with hi/lo splitting: hi*hi, then hi*lo and lo*hi.  a and b
-// are descriptors of the hi parts; the start-address field counts 16-byte
-// units, so a byte offset o is added as o >> 4 (no carry: shared addresses
-// are below 2^18).
-template <bool SPLIT>
-__device__ __forceinline__ void mma3(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, bool acc)
-{
-    tcx::mma_bf16(d, a, b, idesc, acc);
-    if (SPLIT) {
-        tcx::mma_bf16(d, a, b + ((kTcNumMat * kMat) >> 4), idesc, true);
-        tcx::mma_bf16(d, a + (kLo >> 4), b, idesc, true);
-    }
-}
-
-// 8 pixels of one window row: raw load, then exact widening to float (the
-// integer in the low mantissa bits of 2^23, minus 2^23)
-template <typename PixT> struct Raw;
-template <> struct Raw<uint16_t> {
-    using type = uint4;
-    __device__ static uint4 zero() { return make_uint4(0, 0, 0, 0); }
-};
-template <> struct Raw<uint8_t> {
-    using type = uint2;
-    __device__ static uint2 zero() { return make_uint2(0, 0); }
-};
-
-template <typename PixT>
-__device__ __forceinline__ typename Raw<PixT>::type load_raw(const PixT* ptr)
-{
-    return __ldg(reinterpret_cast<const typename Raw<PixT>::type*>(ptr));
-}
-
-template <typename PixT>
-__device__ __forceinline__ void widen8(const typename Raw<PixT>::type& q, float* px, float s);
-
-// s = +1 or -1: the pixels times s (one FMA each, like the subtraction)
-template <>
-__device__ __forceinline__ void widen8<uint16_t>(const uint4& q, float* px, float s)
-{
-    const uint32_t w[4] = { q.x, q.y, q.z, q.w };
-    const float c = -8388608.f * s;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        // bytes {w.b0, w.b1, 0x00, 0x4b} and {w.b2, w.b3, 0x00, 0x4b}
-        px[2 * j] = fmaf(__uint_as_float(__byte_perm(w[j], 0x4b00u, 0x5410u)), s, c);
-        px[2 * j + 1] = fmaf(__uint_as_float(__byte_perm(w[j], 0x4b00u, 0x5432u)), s, c);
-    }
-}
-
-template <>
-__device__ __forceinline__ void widen8<uint8_t>(const uint2& q, float* px, float s)
-{
-    const uint32_t w[2] = { q.x, q.y };
-    const float c = -8388608.f * s;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        px[j] = fmaf(__uint_as_float(__byte_perm(w[0], 0x4b00u, 0x5440u + j)), s, c);
-        px[4 + j] = fmaf(__uint_as_float(__byte_perm(w[1], 0x4b00u, 0x5440u + j)), s, c);
-    }
-}
-
-// VT: vertical tiles, four windows of one grid column (row step <= 8): their
-// rows overlap, so stage 1 transforms each image row once (56 rows per frame
-// instead of 4 x 32) and E1 copies its coefficients into every window that
-// contains the row.  Otherwise four windows of one grid row.
-template <bool SPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
-__global__ void __launch_bounds__(kThreads, 4)
-piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
-{
-    // peak scan range in swapped-plane coordinates (image_utils.impl.h:48,
-    // :54; limited search: rect::dilate(0.5), rect.cpp:109-126)
-    constexpr int D0 = LIMIT ? W / 4 : 0;
-    constexpr int VW = LIMIT ? W / 2 : W;
-    constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
-    constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
-    constexpr uint32_t kIdK32 = tcx::idesc_bf16(128, 32, false);
-    constexpr uint32_t kIdM32 = tcx::idesc_bf16(128, 32, true);
-    // stage 3 has 64 rows: M = 64 puts row r in lane 32 (r / 16) + r % 16,
-    // i.e. window w's 16 rows in the first 16 lanes of warp w
-    constexpr uint32_t kIdK64M64 = tcx::idesc_bf16(64, 64, false);
-    constexpr uint32_t kIdM64 = tcx::idesc_bf16(128, 64, true);
-
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* cst = smem;
-    unsigned char* dat = smem + kConstBytes;
-    float* sums = reinterpret_cast<float*>(dat + kDataBytes);          // [window][frame]
-    int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // window corners
-    int* gwi = reinterpret_cast<int*>(org + 2 * kTile);                 // window indices
-    float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);              // VT: row sums [frame][row]
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(rs + 128);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
-    int* abort_flag = reinterpret_cast<int*>(tslot + 1);
-
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t cst_a = tcx::smem_addr(cst), dat_a = tcx::smem_addr(dat);
-    // descriptors: constant matrix m (hi part; the lo parts follow all hi
-    // parts), and the data buffer in the layouts of the four stages
-    const uint64_t dB = tcx::sdesc(cst_a, 128, 512);
-    auto mat = [&](int m, int ks) { return dB + (uint64_t)((m * kMat + ks * 256) >> 4); };
-    const uint64_t dA1 = tcx::sdesc(dat_a, 128, 512);     // K-major, 4 k-groups per row group
-    const uint64_t dA2 = tcx::sdesc(dat_a, 2048, 128);    // MN-major, k-group stride 2 KB
-    const uint64_t dA3 = tcx::sdesc(dat_a, 128, 1024);    // K-major, 8 k-groups per row group
-    auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
-
-    for (int i = tid; i < kConstBytes / 16; i += kThreads)
-        reinterpret_cast<uint4*>(cst)[i] = consts[i];
-    if (tid == 0) {
-        tcx::mbar_init(mbar, 1);
-        *abort_flag = 0;
-    }
-    if (warp == 0) tcx::tmem_alloc(tslot, kTmemCols);
-    tcx::fence_before();
-    __syncthreads();
-    tcx::fence_after();
-    const uint32_t tbase = *tslot;
-    const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
-
-    const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
-    const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
-    const size_t pitch = p.pitch / sizeof(PixT);
-    // tiles: kTile consecutive windows of one grid column (VT) or row; each
-    // CTA walks a contiguous range of tiles down the grid, so consecutive
-    // tiles share image rows, which the next tile then finds in L1
-    const int gny = (int)(p.n_win / p.gnx);
-    // tiles per walked line: a grid column of VT tiles, a grid row otherwise
-    const int n_line = VT ? p.gnx : gny;
-    const int per_line = VT ? (gny + kTile - 1) / kTile : (p.gnx + kTile - 1) / kTile;
-    const int n_tiles = n_line * per_line;
-    const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
-    const int t_end = (int)((int64_t)(blockIdx.x + 1) * n_tiles / gridDim.x);
-    uint32_t phase = 0;
-
-    // wait for the committed MMAs; a wait that gives up aborts the CTA
-    auto wait_mma = [&]() {
-        if (!tcx::mbar_wait(mbar, phase)) {
-            *abort_flag = 1;
-            if (p.status) atomicExch(p.status, 1);
-        }
-        phase ^= 1u;
-        tcx::fence_after();
-    };
-
-    // item mapping of the pixel stage: 8 consecutive lanes fill one core
-    // matrix (rows R & 7), so the 16-byte stores are conflict-free
-    const int it_r7 = tid & 7, it_g = (tid >> 3) & 3, it_rg = tid >> 5;
-
-    for (int tile = t_begin; tile < t_end; ++tile) {
-        if (tid < 2 * kTile) {   // this tile's windows, then the next tile's; x < 0: no window
-            const int t = tile + (tid >> 2), i = tid & (kTile - 1);
-            int col, row;
-            if (VT) {   // tile t: column t / per_line, rows kTile * (t % per_line) + i
-                const int c = t / per_line;
-                col = c;
-                row = kTile * (t - c * per_line) + i;
-            } else {    // tile t: row t % gny, columns kTile * (t / gny) + i
-                const int c = t / gny;
-                row = t - c * gny;
-                col = kTile * c + i;
-            }
-            const bool ok = t < t_end && col < p.gnx && row < gny;
-            org[tid] = ok ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy) : make_int2(-1, -1);
-            gwi[tid] = row * p.gnx + col;
-        }
-        __syncthreads();
-
-        // number of window rows of this tile (VT: image rows below its top)
-        const int vrows = VT ? (org[1].x >= 0 ? (org[2].x >= 0 ? (org[3].x >= 0 ? 3 : 2) : 1) : 0) * p.gdy + W
-                             : 0;
-        if constexpr (VT) {
-            // ---- stage-1 operand: rows R = f * 64 + y of the tile's image
-            // rows (y < vrows <= 56), K-major 128 x 32 (hi | lo)
-            const int2 o = org[0];
-            typename Raw<PixT>::type raw[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                const int f = t >> 1, y = R & 63;
-                raw[t] = (o.x >= 0 && y < vrows)
-                             ? load_raw<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g)
-                             : Raw<PixT>::zero();
-            }
-            const float sb = (it_r7 & 1) ? -1.f : 1.f;   // frame B rows times (-1)^y
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                float px[8];
-                widen8<PixT>(raw[t], px, (t >> 1) ? sb : 1.f);
-                put8<SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
-            }
-        } else {
-        // ---- stage-1 operand: window rows, K-major 256 x 32 (hi | lo);
-        // rows R = (2 m1 + wl) * 64 + f * 32 + y.  All eight loads are in
-        // flight before the first conversion.
-            typename Raw<PixT>::type raw[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
-                const int2 o = org[w];
-                raw[t] = (o.x >= 0)
-                             ? load_raw<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g)
-                             : Raw<PixT>::zero();
-            }
-            // frame B rows times (-1)^y: its column spectrum comes out rotated
-            // by 16 in k_y (see E2); rows R have f = t & 1, y & 1 = R & 1
-            const float sb = (it_r7 & 1) ? -1.f : 1.f;
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                float px[8];
-                widen8<PixT>(raw[t], px, (t & 1) ? sb : 1.f);
-                put8<SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
-            }
-        }
-        tcx::fence_proxy();
-        tcx::fence_before();
-        __syncthreads();
-        if (*abort_flag) break;
-
-        // ---- stage 1: H = X * G, one (VT) or two M-tiles of 128 rows
-        if (tid == 0) {
-            tcx::fence_after();
-#pragma unroll
-            for (int m1 = 0; m1 < (VT ? 1 : 2); ++m1)
-#pragma unroll
-                for (int ks = 0; ks < 2; ++ks)
-                    mma3<SPLIT>(tbase + 32 * m1, dA1 + off(m1 * 8192 + ks * 256), mat(kTcG1, ks),
-                                kIdK32, ks > 0);
-            tcx::commit(mbar);
-        }
-        // the next tile's window rows into L2 while this tile computes
-        if constexpr (VT) {
-            const int2 o = org[kTile];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                const int f = t >> 1, y = R & 63;
-                if (o.x >= 0 && y < 56 && o.y + y < p.img_h) {
-                    const PixT* q = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g;
-                    asm volatile("prefetch.global.L2 [%0];" :: "l"(q));
-                }
-            }
-        } else {
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
-                const int2 o = org[kTile + w];
-                if (o.x >= 0) {
-                    const PixT* q = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g;
-                    asm volatile("prefetch.global.L2 [%0];" :: "l"(q));
-                }
-            }
-        }
-        wait_mma();
-
-        if constexpr (VT) {
-            // ---- E1: each image row's coefficients into every window that
-            // contains it (stage-2 operand, MN-major, rows (window, frame, k)
-            // = 128, K = (U | V) x window row = 64); row sums into rs
-            float c[32];
-            tcx::tmem_ld32(tlane, c);
-            const int f = warp >> 1, y = (warp & 1) * 32 + lane;
-            if (y < vrows) {
-                rs[f * 64 + y] = (f && (y & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
-                uint4 hi[4], lo[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (SPLIT) split8(c + 8 * q, hi[q], lo[q]);
-                    else hi[q] = round8(c + 8 * q);
-                }
-#pragma unroll
-                for (int i = 0; i < kTile; ++i) {
-                    const int yl = y - i * p.gdy;
-                    if (org[i].x >= 0 && yl >= 0 && yl < W) {
-                        const int g0 = (i * 32 + f * 16) >> 3;
-#pragma unroll
-                        for (int part = 0; part < 2; ++part) {
-                            const int k = part * 32 + yl;
-                            const int base = (k >> 3) * 2048 + (k & 7) * 16;
-#pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                *reinterpret_cast<uint4*>(dat + base + (g0 + h) * 128) = hi[2 * part + h];
-                                if (SPLIT) *reinterpret_cast<uint4*>(dat + kLo + base + (g0 + h) * 128) = lo[2 * part + h];
-                            }
-                        }
-                    }
-                }
-            }
-        } else {
-        // ---- E1: coefficients -> stage-2 operand (MN-major, rows
-        // (window, frame, k) = 128, K = (U | V) x y = 64); row sums
-        float c2[64];
-        tcx::tmem_ld32x2(tlane, tlane + 32, c2, c2 + 32);
-#pragma unroll
-        for (int m1 = 0; m1 < 2; ++m1) {
-            const float* c = c2 + 32 * m1;
-            const int w = 2 * m1 + (warp >> 1), f = warp & 1;
-            float s = (f && (lane & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) sums[2 * w + f] = s;
-            const int g0 = (w * 32 + f * 16) >> 3;
-#pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                const int k = part * 32 + lane;
-                const int base = (k >> 3) * 2048 + (k & 7) * 16;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) put8<SPLIT>(dat, base + (g0 + h) * 128, c + part * 16 + h * 8);
-            }
-        }
-        }
-        tcx::fence_proxy();
-        tcx::fence_before();
-        __syncthreads();
-        if (VT && tid >= 32 && tid < 32 + 2 * kTile) {   // window sums from the row sums
-            const int i = (tid - 32) >> 1, f = tid & 1;
-            float s = 0.f;
-            if (org[i].x >= 0)
-                for (int yl = 0; yl < W; ++yl) s += rs[f * 64 + i * p.gdy + yl];
-            sums[2 * i + f] = s;
-        }
-
-        // ---- stage 2: conj of the column DFT: Re = U*C + V*(-S),
-        // -Im = U*S + V*C
-        if (tid == 0) {   // N = 64: the U part against [C; S], the V part against [-S; C]
-            tcx::fence_after();
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dA2 + off(ks * 4096), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdM64,
-                            ks > 0);
-            tcx::commit(mbar);
-        }
-        wait_mma();
-
-        // ---- E2: products into the stage-3 operand (K-major, rows
-        // (window, k_x) = 64, K = (Re | Im) x k_y = 64).  Warp w holds
-        // window w: lane = frame * 16 + k_x.
-        {
-            const int w = warp;
-            const int f = lane >> 4, kxr = lane & 15;
-            float x[64];   // [k_y] = Re X, [32 + k_y] = -Im X of this lane's (frame, k_x)
-            tcx::tmem_ld32x2(tlane, tlane + 32, x, x + 32);
-            // k_x slot 0 rows of both frames for the packed bins
-            float* pk = reinterpret_cast<float*>(dat + kPacked) + warp * 128;
-            if (kxr == 0) {
-#pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    *reinterpret_cast<float4*>(pk + f * 64 + 4 * j) =
-                        make_float4(x[4 * j], x[4 * j + 1], x[4 * j + 2], x[4 * j + 3]);
-            }
-            // frame a's lane computes k_y = j, frame b's k_y = 16 + j (j < 16).
-            // Frame b's columns are rotated by 16 (its rows were multiplied by
-            // (-1)^y), so both lanes find their own values at [j], [32 + j]
-            // and send their partner (lane ^ 16) the values at [16 + j],
-            // [48 + j].  With m = own, o = partner values and n = -Im:
-            // Re P = m_r o_r + m_n o_n, Im P = +-(o_r m_n - o_n m_r), the
-            // sign + for frame a (A = m) and - for frame b (A = o).
-            const float sq = f ? -1.f : 1.f;
-            float pr[16], pi[16];
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const float mr = x[j], mn = x[32 + j];
-                const float orr = __shfl_xor_sync(0xffffffffu, x[16 + j], 16);
-                const float onn = __shfl_xor_sync(0xffffffffu, x[48 + j], 16);
-                float r = fmaf(mr, orr, mn * onn);
-                float q = sq * fmaf(orr, mn, -(onn * mr));
-                if (j & 1) { r = -r; q = -q; }   // quadrant sign (-1)^k_y
-                if (MODE == kModeReal && j == 0) { r = 0.f; q = 0.f; }   // k_y = 0 or 16
-                pr[j] = r;
-                pi[j] = q;
-            }
-            if (kxr != 0) {
-                const int R3 = w * 16 + kxr;
-#pragma unroll
-                for (int part = 0; part < 2; ++part)
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int k = part * 32 + 16 * f + 8 * h;
-                        put8<SPLIT>(dat, ((R3 >> 3) * 8 + (k >> 3)) * 128 + (R3 & 7) * 16,
-                                    (part ? pi : pr) + 8 * h);
-                    }
-            }
-            __syncwarp();
-            // packed row k_x = 0 | 16, one k_y per lane
-            {
-                const int ky = lane, kn = (32 - lane) & 31;
-                const float* sa = pk;          // frame a, k_x slot 0
-                const float* sb = pk + 64;     // frame b, columns rotated by 16
-                const int kb = (ky + 16) & 31, kbn = (kn + 16) & 31;
-                // Z[k] = Re + i Im with Im = -stored
-                const float zar = sa[ky], zai = -sa[32 + ky], zanr = sa[kn], zani = -sa[32 + kn];
-                const float zbr = sb[kb], zbi = -sb[32 + kb], zbnr = sb[kbn], zbni = -sb[32 + kbn];
-                // X0 = (Z[k] + conj Z[-k]) / 2, X16 = i (Z[k] - conj Z[-k]) / 2
-                const float a0r = 0.5f * (zar + zanr), a0i = 0.5f * (zai - zani);
-                const float a6r = -0.5f * (zai + zani), a6i = 0.5f * (zar - zanr);
-                const float b0r = 0.5f * (zbr + zbnr), b0i = 0.5f * (zbi - zbni);
-                const float b6r = -0.5f * (zbi + zbni), b6i = 0.5f * (zbr - zbnr);
-                // P = B conj(A)
-                float p0r = b0r * a0r + b0i * a0i, p0i = b0i * a0r - b0r * a0i;
-                float p6r = b6r * a6r + b6i * a6i, p6i = b6i * a6r - b6r * a6i;
-                if (MODE == kModeReal) {
-                    p0r = 0.f; p0i = 0.f;
-                    if (ky == 0 || ky == 16) { p6r = 0.f; p6i = 0.f; }
-                } else if (ky == 0) {
-                    p0r = 0.f; p0i = 0.f;         // pedestal removed
-                }
-                // packed P(ky, 0) + i P(ky, 16), quadrant sign
-                float r = p0r - p6i, q = p0i + p6r;
-                if (ky & 1) { r = -r; q = -q; }
-                const int R0 = w * 16;
-                put1<SPLIT>(dat, ((R0 >> 3) * 8 + (ky >> 3)) * 128 + (ky & 7) * 2, r);
-                put1<SPLIT>(dat, ((R0 >> 3) * 8 + ((32 + ky) >> 3)) * 128 + (ky & 7) * 2, q);
-            }
-        }
-        tcx::fence_proxy();
-        tcx::fence_before();
-        __syncthreads();
-
-        // ---- stage 3: inverse column DFT, Re T = Pr*C + Pi*(-S),
-        // Im T = Pr*S + Pi*C (M = 64)
-        if (tid == 0) {   // N = 64: the Pr part against [C; S], the Pi part against [-S; C]
-            tcx::fence_after();
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dA3 + off(ks * 256), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdK64M64,
-                            ks > 0);
-            tcx::commit(mbar);
-        }
-        wait_mma();
-
-        // ---- E3: T into the stage-4 operand (MN-major, rows (window, y') =
-        // 128, K = (Re | Im) x k_x = 32); warp w, lanes 0..15 = k_x
-        {
-            const int w = warp, kxr = lane;
-            float t2[64];
-            tcx::tmem_ld32x2(tlane, tlane + 32, t2, t2 + 32);
-            if (lane < 16)
-#pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                const int k = part * 16 + kxr;
-                const int base = (k >> 3) * 2048 + (k & 7) * 16;
-#pragma unroll
-                for (int g = 0; g < 4; ++g) put8<SPLIT>(dat, base + (w * 4 + g) * 128, t2 + 32 * part + 8 * g);
-            }
-        }
-        tcx::fence_proxy();
-        tcx::fence_before();
-        __syncthreads();
-
-        // ---- stage 4: real inverse row DFT, D = T * C4
-        if (tid == 0) {
-            tcx::fence_after();
-#pragma unroll
-            for (int ks = 0; ks < 2; ++ks)
-                mma3<SPLIT>(tbase, dA2 + off(ks * 4096), mat(kTcC4, ks), kIdM32, ks > 0);
-            tcx::commit(mbar);
-        }
-        wait_mma();
-
-        // ---- E4: find_peaks(plane, 2, 1), fit, vector; warp w, row y' = lane
-        {
-            float* pl = reinterpret_cast<float*>(dat) + warp * (32 * kPRow);
-            const int w = warp;
-            const int gw = gwi[w];
-            const int y = lane;
-            float v[32];
-            tcx::tmem_ld32(tlane, v);
-            // strict 4-neighbour maxima of this row (rows above and below
-            // from the neighbouring lanes), then the top two by a pairwise
-            // tree (ties: the lower column)
-            constexpr int NX = SX1 - SX0;
-            float T0[NX], T1[NX];
-            int I0[NX];
-            {
-#pragma unroll
-                for (int x = SX0; x < SX1; ++x) {
-                    const float c = v[x];
-                    const float up = __shfl_up_sync(0xffffffffu, c, 1);
-                    const float dn = __shfl_down_sync(0xffffffffu, c, 1);
-                    const float m = fmaxf(fmaxf(up, dn), fmaxf(v[x - 1], v[x + 1]));
-                    T0[x - SX0] = (m < c) ? c : TC_NEG_INF;
-                    T1[x - SX0] = TC_NEG_INF;
-                    I0[x - SX0] = x;
-                }
-#pragma unroll
-                for (int st = 1; st < NX; st *= 2)
-#pragma unroll
-                    for (int i = 0; i + st < NX; i += 2 * st) {
-                        const bool gt = T0[i + st] > T0[i];
-                        const float lo = fminf(T0[i], T0[i + st]);
-                        T1[i] = fmaxf(fmaxf(T1[i], T1[i + st]), lo);
-                        I0[i] = gt ? I0[i + st] : I0[i];
-                        T0[i] = gt ? T0[i + st] : T0[i];
-                    }
-            }
-            const bool row_in = y >= SY0 && y < SY1;
-            float t0 = row_in ? T0[0] : TC_NEG_INF, t1 = row_in ? T1[0] : TC_NEG_INF;
-            const int tx = I0[0];
-            const bool valid = org[w].x >= 0;
-            if (p.planes && valid) {
-#pragma unroll
-                for (int x = 0; x < W; ++x) p.planes[(size_t)gw * (W * W) + y * W + x] = v[x];
-            }
-            int key = y * W + tx;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float o0 = __shfl_xor_sync(0xffffffffu, t0, o);
-                const float o1 = __shfl_xor_sync(0xffffffffu, t1, o);
-                const int ok = __shfl_xor_sync(0xffffffffu, key, o);
-                const bool take = (o0 > t0) || (o0 == t0 && ok < key);
-                const float n1 = take ? fmaxf(t0, o1) : fmaxf(t1, o0);
-                t0 = take ? o0 : t0;
-                key = take ? ok : key;
-                t1 = n1;
-            }
-            // fit_simple_gaussian: the peak row and its neighbours into
-            // shared memory, six logarithms on six lanes, relative to the
-            // pedestal sum(a) sum(b)
-            const int px = key & (W - 1), py = key >> 5;
-            if (y >= py - 1 && y <= py + 1) {
-#pragma unroll
-                for (int j = 0; j < 8; ++j)
-                    *reinterpret_cast<float4*>(pl + y * kPRow + 4 * j) =
-                        make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
-            }
-            __syncwarp();
-            // REAL mode: the reference's unpack zeroes spectrum row 0, so its
-            // plane has no pedestal
-            const float ped = MODE == kModeReal ? 0.f : sums[2 * w] * sums[2 * w + 1];
-            const int j = lane < 6 ? lane : 0;
-            // numerator / denominator positions of lane j's logarithm
-            const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
-            const int ny = (j == 3 || j == 4) ? py - 1 : (j == 5 ? py + 1 : py);
-            const int qx = (j == 0) ? px + 1 : px;
-            const int qy = (j == 3) ? py + 1 : py;
-            const float an = pl[(ny & 31) * kPRow + (nx & 31)];
-            const float ad = pl[(qy & 31) * kPRow + (qx & 31)];
-            const float lg = log1pf((an - ad) / (ad + ped));
-            const float lxr = __shfl_sync(0xffffffffu, lg, 0);
-            const float lxl = __shfl_sync(0xffffffffu, lg, 1);
-            const float lxrr = __shfl_sync(0xffffffffu, lg, 2);
-            const float lyd = __shfl_sync(0xffffffffu, lg, 3);
-            const float lyu = __shfl_sync(0xffffffffu, lg, 4);
-            const float lydd = __shfl_sync(0xffffffffu, lg, 5);
-            if (lane == 0 && valid) {
-                opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
-                int32_t code = -1;
-                const int2 o = org[w];
-                const bool has2 = t1 > TC_NEG_INF;
-                if (has2) {
-                    const float vc = pl[py * kPRow + px];
-                    const float C = vc + ped;
-                    const float L = pl[py * kPRow + px - 1] + ped, R = pl[py * kPRow + px + 1] + ped;
-                    const float U = pl[(py - 1) * kPRow + px] + ped, D = pl[(py + 1) * kPRow + px] + ped;
-                    const float nan = __int_as_float(0x7fffffff);
-                    const bool okx = L > 0.f && C > 0.f && R > 0.f;
-                    const bool oky = U > 0.f && C > 0.f && D > 0.f;
-                    const float fx = okx ? lxr / (2.f * (lxl + lxrr)) : nan;
-                    const float fy = oky ? lyd / (2.f * (lyu + lydd)) : nan;
-                    const float p0 = t0 + ped, p1 = t1 + ped;
-                    out.x = (float)(o.x + W / 2);
-                    out.y = (float)(p.img_h - (o.y + W / 2));
-                    out.u = (float)(W / 2 - px) - fx;
-                    out.v = (float)(W / 2 - py) - fy;
-                    out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
-                    code = key;
-                }
-                p.out_vec[gw] = out;
-                if (p.out_peak) p.out_peak[gw] = code;
-                if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sums[2 * w] * (double)sums[2 * w + 1];
-            }
-        }
-        tcx::fence_before();
-        __syncthreads();
-    }
-    tcx::fence_before();
-    __syncthreads();
-    tcx::fence_after();
-    if (warp == 0) tcx::tmem_dealloc(tbase, kTmemCols);
-}
-
-template <bool SPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
-cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
-{
-    auto kern = piv_tc_kernel<SPLIT, MODE, LIMIT, PixT, VT>;
-    static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
-    static std::atomic<int> sm_count[64];
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const uint64_t bit = 1ull << (dev & 63);
-    if (!(attr_done.load() & bit)) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        if (e != cudaSuccess) return e;
-        int sms = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        sm_count[dev & 63].store(sms);
-        attr_done.fetch_or(bit);
-    }
-    const int64_t gny = p.n_win / p.gnx;
-    const int64_t tiles = VT ? (int64_t)p.gnx * ((gny + kTile - 1) / kTile)
-                             : gny * ((p.gnx + kTile - 1) / kTile);
-    const int64_t cap = 4 * (int64_t)sm_count[dev & 63].load();
-    const int blocks = (int)(tiles < cap ? tiles : cap);
-    if (blocks <= 0) return cudaSuccess;
-    kern<<<blocks, kThreads, kSmemBytes, s>>>(p, reinterpret_cast<const uint4*>(consts));
-    return cudaGetLastError();
-}
-
-template <bool SPLIT, int MODE, bool LIMIT>
-cudaError_t by_dtype(const PivParams& p, int dtype, const void* consts, cudaStream_t s)
-{
-    const bool vt = p.gdy > 0 && p.gdy <= 8;   // four stacked windows span <= 56 rows
-    if (dtype == kU8)
-        return vt ? launch_t<SPLIT, MODE, LIMIT, uint8_t, true>(p, consts, s)
-                  : launch_t<SPLIT, MODE, LIMIT, uint8_t, false>(p, consts, s);
-    return vt ? launch_t<SPLIT, MODE, LIMIT, uint16_t, true>(p, consts, s)
-              : launch_t<SPLIT, MODE, LIMIT, uint16_t, false>(p, consts, s);
-}
-
-template <bool SPLIT>
-cudaError_t by_mode(const PivParams& p, int dtype, int mode, int limit, const void* consts,
-                    cudaStream_t s)
-{
-    if (mode == kModeReal)
-        return limit ? by_dtype<SPLIT, kModeReal, true>(p, dtype, consts, s)
-                     : by_dtype<SPLIT, kModeReal, false>(p, dtype, consts, s);
-    return limit ? by_dtype<SPLIT, kModeComplex, true>(p, dtype, consts, s)
-                 : by_dtype<SPLIT, kModeComplex, false>(p, dtype, consts, s);
-}
-
-// ---- host: the constant matrices ----------------------------------------------
+// BF16: round to nearest even (finite inputs)
 uint16_t bf16_bits(float f)
 {
-    // round to nearest even (finite inputs)
     uint32_t u;
     std::memcpy(&u, &f, 4);
     const uint32_t r = u + 0x7fffu + ((u >> 16) & 1u);
@@ -770,49 +43,95 @@ float bf16_value(uint16_t h)
     return f;
 }
 
+// FP16 (IEEE binary16): round to nearest even, subnormals kept, |f| < 65504
+uint16_t fp16_bits(float f)
+{
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const int e8 = (int)((x >> 23) & 0xffu);
+    uint32_t mant = x & 0x7fffffu;
+    if (e8 == 0) return (uint16_t)sign;
+    const int e = e8 - 127 + 15;
+    if (e >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (e <= 0) {
+        if (e < -10) return (uint16_t)sign;
+        mant |= 0x800000u;
+        const int shift = 14 - e;
+        uint32_t h = mant >> shift;
+        const uint32_t rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (h & 1u))) ++h;
+        return (uint16_t)(sign | h);
+    }
+    uint32_t h = ((uint32_t)e << 10) | (mant >> 13);
+    const uint32_t rem = mant & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+    return (uint16_t)(sign | h);
+}
+
+float fp16_value(uint16_t h)
+{
+    const int e = (h >> 10) & 0x1f;
+    const int m = h & 0x3ff;
+    const float v = e == 0 ? std::ldexp((float)m, -24) : std::ldexp((float)(1024 + m), e - 25);
+    return (h & 0x8000u) ? -v : v;
+}
+
 }  // namespace tc
 
 bool tc_supports(int w, int dtype) { return w == 32 && (dtype == kU8 || dtype == kU16); }
 
-size_t tc_constant_bytes() { return (size_t)tc::kConstBytes; }
+size_t tc_constant_bytes() { return 2 * (size_t)tc::kSetBytes; }
 
+// Two sets: BF16, then FP16 (the FP16 stage-1 matrix scaled by 2^-9).
 void tc_constants(unsigned char* out)
 {
     using namespace tc;
     const double pi = 3.14159265358979323846;
-    auto put = [&](int m, int n, int k, double v) {
-        const uint16_t hi = bf16_bits((float)v);
-        const uint16_t lo = bf16_bits((float)(v - (double)bf16_value(hi)));
-        std::memcpy(out + m * kMat + kmaj32(n, k), &hi, 2);
-        std::memcpy(out + (kTcNumMat + m) * kMat + kmaj32(n, k), &lo, 2);
-    };
-    for (int n = 0; n < 32; ++n)
-        for (int k = 0; k < 32; ++k) {
-            // stage 1, B[k = x][n = coefficient]
-            double g;
-            if (n < 16) g = std::cos(2 * pi * n * k / 32.0);
-            else if (n == 16) g = (k & 1) ? -1.0 : 1.0;
-            else g = std::sin(2 * pi * (n - 16) * k / 32.0);
-            put(kTcG1, n, k, g);
-            const double c = std::cos(2 * pi * n * k / 32.0), s = std::sin(2 * pi * n * k / 32.0);
-            put(kTcC, n, k, c);
-            put(kTcS, n, k, s);
-            put(kTcNS, n, k, -s);
-            // stage 4, B[k = (part, k_x)][n = x'], x = (x' + 16) mod 32
-            const int x = (n + 16) & 31;
-            const int part = k >> 4, kx = k & 15;
-            double v;
-            if (part == 0) v = kx == 0 ? 1.0 : 2.0 * std::cos(2 * pi * kx * x / 32.0);
-            else v = kx == 0 ? ((x & 1) ? -1.0 : 1.0) : -2.0 * std::sin(2 * pi * kx * x / 32.0);
-            put(kTcC4, n, k, v);
-        }
+    for (int set = 0; set < 2; ++set) {
+        unsigned char* o = out + set * kSetBytes;
+        auto put = [&](int m, int n, int k, double v) {
+            uint16_t hi, lo;
+            if (set == 0) {
+                hi = bf16_bits((float)v);
+                lo = bf16_bits((float)(v - (double)bf16_value(hi)));
+            } else {
+                hi = fp16_bits((float)v);
+                lo = fp16_bits((float)(v - (double)fp16_value(hi)));
+            }
+            std::memcpy(o + m * kMat + kmaj32(n, k), &hi, 2);
+            std::memcpy(o + (kTcNumMat + m) * kMat + kmaj32(n, k), &lo, 2);
+        };
+        const double gscale = set == 0 ? 1.0 : 1.0 / 512.0;
+        for (int n = 0; n < 32; ++n)
+            for (int k = 0; k < 32; ++k) {
+                // stage 1, B[k = x][n = coefficient]
+                double g;
+                if (n < 16) g = std::cos(2 * pi * n * k / 32.0);
+                else if (n == 16) g = (k & 1) ? -1.0 : 1.0;
+                else g = std::sin(2 * pi * (n - 16) * k / 32.0);
+                put(kTcG1, n, k, g * gscale);
+                const double c = std::cos(2 * pi * n * k / 32.0), s = std::sin(2 * pi * n * k / 32.0);
+                put(kTcC, n, k, c);
+                put(kTcS, n, k, s);
+                put(kTcNS, n, k, -s);
+                // stage 4, B[k = (part, k_x)][n = x'], x = (x' + 16) mod 32
+                const int x = (n + 16) & 31;
+                const int part = k >> 4, kx = k & 15;
+                double v;
+                if (part == 0) v = kx == 0 ? 1.0 : 2.0 * std::cos(2 * pi * kx * x / 32.0);
+                else v = kx == 0 ? ((x & 1) ? -1.0 : 1.0) : -2.0 * std::sin(2 * pi * kx * x / 32.0);
+                put(kTcC4, n, k, v);
+            }
+    }
 }
 
-cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split,
+cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
                           const void* consts, cudaStream_t s)
 {
-    return split ? tc::by_mode<true>(p, dtype, mode, limit, consts, s)
-                 : tc::by_mode<false>(p, dtype, mode, limit, consts, s);
+    const unsigned char* c = static_cast<const unsigned char*>(consts);
+    return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, c + tc::kSetBytes, s)
+                : launch_piv_tc_bf16(p, dtype, mode, limit, split, c, s);
 }
 
 }  // namespace opiv

@@ -29,11 +29,12 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t 
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
 }
 
-// Instruction descriptor of kind::f16 with BF16 operands and an FP32
-// accumulator; a_mn selects an MN-major A operand (B is K-major).
-__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n, bool a_mn)
+// Instruction descriptor of kind::f16 with an FP32 accumulator and BF16
+// (f16 = false) or FP16 operands (A and B of the same type); a_mn selects an
+// MN-major A operand (B is K-major).
+__host__ __device__ constexpr uint32_t idesc_f16kind(int m, int n, bool a_mn, bool f16)
 {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) |
+    return (1u << 4) | ((f16 ? 0u : 1u) << 7) | ((f16 ? 0u : 1u) << 10) | ((a_mn ? 1u : 0u) << 15) |
            ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 

@@ -39,6 +39,7 @@ ERR_CUDA = -12
 ERR_NO_DEVICE = -13
 ERR_TIMEOUT = -14
 PREC_FP32, PREC_TC_SPLIT_BF16, PREC_TC_BF16, PREC_FP64 = 0, 1, 2, 3
+PREC_TC_SPLIT_FP16, PREC_TC_FP16 = 4, 5
 
 DTYPES = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
 SYMBOLS = [
@@ -275,8 +276,8 @@ class Plan:
 
     def set_precision(self, precision: int):
         """PREC_FP32 (default, reference-exact peaks), PREC_TC_SPLIT_BF16,
-        PREC_TC_BF16 (tensor cores, 32 x 32 windows) or PREC_FP64 (every
-        window through the exact kernel)."""
+        PREC_TC_BF16, PREC_TC_SPLIT_FP16, PREC_TC_FP16 (tensor cores, 32 x 32
+        windows) or PREC_FP64 (every window through the exact kernel)."""
         _check(load().opiv_plan_set_precision(self._h, precision))
 
     def status(self):

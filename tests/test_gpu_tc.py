@@ -16,6 +16,12 @@ SPLIT_PLANE_RTOL = 2e-5
 SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH = 1e-4, 1e-3, 1e-4
 # plain BF16: the target itself
 BF16_RMS, BF16_MAX, BF16_MISMATCH = 0.01, 0.05, 5e-3
+# plain FP16 (11-bit significand, scaled): between the two
+FP16_RMS, FP16_MAX, FP16_MISMATCH = 1e-3, 1e-2, 1e-3
+BOUNDS = {og.PREC_TC_SPLIT_BF16: (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH),
+          og.PREC_TC_BF16: (BF16_RMS, BF16_MAX, BF16_MISMATCH),
+          og.PREC_TC_SPLIT_FP16: (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH),
+          og.PREC_TC_FP16: (FP16_RMS, FP16_MAX, FP16_MISMATCH)}
 
 
 def _torch():
@@ -58,12 +64,14 @@ def displacement_error(got, ref):
 
 
 @pytest.mark.parametrize("precision,rtol", [(og.PREC_TC_SPLIT_BF16, SPLIT_PLANE_RTOL),
-                                            (og.PREC_TC_BF16, 1e-2)])
+                                            (og.PREC_TC_BF16, 1e-2),
+                                            (og.PREC_TC_SPLIT_FP16, SPLIT_PLANE_RTOL),
+                                            (og.PREC_TC_FP16, 2e-3)])
 def test_planes_match_fp64_fft(precision, rtol):
     a, b = synth.config1()
     got = run(a, b, 16, precision, planes=True)
     ref, ped = reference_planes(a, b, got["grid"])
-    if precision == og.PREC_TC_SPLIT_BF16:
+    if precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT_FP16):
         assert np.array_equal(got["ped"], ped)     # exact: integer sums below 2^24
     err = np.abs(got["planes"] - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
     assert err.max() <= rtol, f"plane error {err.max():.3e} of the plane peak"
@@ -74,8 +82,7 @@ def test_vectors_against_fp64_pass(mode):
     """config-2 statistics on a 1024^2 crop (16,129 windows at step 8)."""
     a, b = synth.config2(size=1024)
     ref = run(a, b, 8, og.PREC_FP64, mode=mode)
-    for precision, (rms_t, max_t, mm_t) in ((og.PREC_TC_SPLIT_BF16, (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH)),
-                                            (og.PREC_TC_BF16, (BF16_RMS, BF16_MAX, BF16_MISMATCH))):
+    for precision, (rms_t, max_t, mm_t) in BOUNDS.items():
         got = run(a, b, 8, precision, mode=mode)
         assert np.array_equal(got["vec"][:, :2], ref["vec"][:, :2]), "window centres differ"
         rms, mx, mm = displacement_error(got, ref)
@@ -142,8 +149,7 @@ def test_precision_sweep_variants(variant):
     field, 1024^2 crop: both tensor-core precisions inside the target."""
     a, b = synth.config4(variant, size=1024)
     ref = run(a, b, 8, og.PREC_FP64)
-    for precision, (rms_t, max_t, mm_t) in ((og.PREC_TC_SPLIT_BF16, (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH)),
-                                            (og.PREC_TC_BF16, (BF16_RMS, BF16_MAX, BF16_MISMATCH))):
+    for precision, (rms_t, max_t, mm_t) in BOUNDS.items():
         got = run(a, b, 8, precision)
         rms, mx, mm = displacement_error(got, ref)
         assert rms <= rms_t and mx <= max_t and mm <= mm_t, (variant, precision, rms, mx, mm)
