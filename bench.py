@@ -598,6 +598,117 @@ def run_sweep(args):
                       "rows": rows}), flush=True)
 
 
+# ---- adjoint and uncertainty ------------------------------------------------------
+def run_adjoint(args):
+    """The config-5 workload: a 2048^2 float32 pair (0.02 ppp, shift (0.40,
+    0.25), noise sigma 0.02), 32 px windows at step 16 (16,129 windows).
+    The adjoint of every vector against FP64 central differences through
+    the oracle (h = 1e-3, 256 sampled windows, the 4 pixels with the
+    largest adjoint entries of frame A each), and the propagated sigma_u,
+    sigma_v against Monte Carlo over 1000 noise seeds."""
+    import torch
+
+    import opiv_gb300 as og
+    from opiv_gb300 import synth
+    from oracle import oracle
+
+    torch.cuda.set_device(0)
+    size, ia, step, sig = 2048, 32, 16, 0.02
+    a, b = synth.config5(size=size)
+    plan = og.Plan(size, size, np.float32, ia, step)
+    da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    pitch = size * 4
+    vec = torch.empty((plan.n, 5), dtype=torch.float32, device="cuda")
+    pk = torch.empty(plan.n, dtype=torch.int32, device="cuda")
+    plan.process_device(da.data_ptr(), db.data_ptr(), pitch, vec.data_ptr(), pk.data_ptr(), 0)
+    torch.cuda.synchronize()
+    grid = plan.grid()
+    pkn = pk.cpu().numpy()
+    rng = np.random.default_rng(5)
+    nx = len(np.unique(grid[:, 0]))
+    # 256 windows on a lattice of every 4th window: no two share a pixel
+    lattice = np.arange(plan.n).reshape(-1, nx)[::4, ::4].ravel()
+    lattice = lattice[pkn[lattice] >= 0]
+    sample = np.sort(rng.choice(lattice, size=min(256, len(lattice)), replace=False))
+    cot = torch.zeros((plan.n, 2), dtype=torch.float32, device="cuda")
+    cot[torch.from_numpy(sample).cuda(), 0] = 1.0
+    ga = torch.zeros_like(da)
+    gb = torch.zeros_like(db)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    plan.adjoint_device(da.data_ptr(), db.data_ptr(), pitch, pk.data_ptr(), cot.data_ptr(),
+                        ga.data_ptr(), gb.data_ptr(), pitch)
+    ev1.record()
+    torch.cuda.synchronize()
+    vjp_ms = ev0.elapsed_time(ev1)
+    gan = ga.cpu().numpy()
+    orc = oracle.get("port")
+    h, errs = 1e-3, []
+    for w in sample:
+        x, y = grid[w]
+        wa = a[y:y + ia, x:x + ia].astype(np.float64)
+        wb = b[y:y + ia, x:x + ia].astype(np.float64)
+        g = gan[y:y + ia, x:x + ia]
+        for flat in np.argsort(-np.abs(g).ravel())[:4]:
+            py, px = divmod(int(flat), ia)
+            us = []
+            for sgn in (1, -1):
+                wp = wa.copy()
+                wp[py, px] += sgn * h
+                us.append(orc.process_windows(wp, wb, np.array([[0, 0]], np.int32), ia,
+                                              og.CORR_COMPLEX)[0][0, 2])
+            fd = (us[0] - us[1]) / (2 * h)
+            if np.isfinite(fd):
+                errs.append(abs(fd - g[py, px]) / max(abs(fd), 1e-3))
+    errs = np.array(errs)
+
+    # propagated sigma at the clean pair against Monte Carlo over noise seeds
+    a0, b0 = synth.config5(size=size, noise=0.0)
+    c0a, c0b = torch.from_numpy(a0).cuda(), torch.from_numpy(b0).cuda()
+    plan.process_device(c0a.data_ptr(), c0b.data_ptr(), pitch, vec.data_ptr(), pk.data_ptr(), 0)
+    dsig = torch.zeros((plan.n, 2), dtype=torch.float32, device="cuda")
+    ev0.record()
+    plan.adjoint_device(c0a.data_ptr(), c0b.data_ptr(), pitch, pk.data_ptr(), var_a=sig * sig,
+                        var_b=sig * sig, d_sigma=dsig.data_ptr())
+    ev1.record()
+    torch.cuda.synchronize()
+    sigma_ms = ev0.elapsed_time(ev1)
+    pred = dsig.cpu().numpy()
+    pk0 = pk.cpu().numpy()
+    gen = torch.Generator(device="cuda").manual_seed(20261203 + 5000)
+    s1 = torch.zeros((plan.n, 2), dtype=torch.float64, device="cuda")
+    s2 = torch.zeros_like(s1)
+    same = torch.ones(plan.n, dtype=torch.bool, device="cuda")
+    dpk = torch.empty_like(pk)
+    pk0d = pk.clone()
+    seeds = args.mc_seeds
+    for _ in range(seeds):
+        na = c0a + sig * torch.randn(c0a.shape, generator=gen, device="cuda")
+        nb = c0b + sig * torch.randn(c0b.shape, generator=gen, device="cuda")
+        plan.process_device(na.data_ptr(), nb.data_ptr(), pitch, vec.data_ptr(), dpk.data_ptr(), 0)
+        uv = vec[:, 2:4].double()
+        s1 += uv
+        s2 += uv * uv
+        same &= dpk == pk0d
+    mean = s1 / seeds
+    mc = torch.sqrt(torch.clamp(s2 / seeds - mean * mean, min=0) * seeds / (seeds - 1)).cpu().numpy()
+    ok = same.cpu().numpy() & (pk0 >= 0) & np.isfinite(pred).all(1) & (pred > 0).all(1) & np.isfinite(mc).all(1)
+    ratio = mc[ok] / pred[ok]
+    q = np.percentile(ratio, [25, 50, 75], axis=0)
+    print(json.dumps({
+        "metric": "adjoint and propagated uncertainty", "workload": "config5_2048sq_f32_ia32_step16",
+        "windows": plan.n, "vjp_ms": vjp_ms, "sigma_ms": sigma_ms,
+        "fd_check": {"windows": int(len(sample)), "pixels": int(len(errs)), "h": h,
+                     "rel_err_median": float(np.median(errs)), "rel_err_p99": float(np.percentile(errs, 99)),
+                     "rel_err_max": float(errs.max())},
+        "monte_carlo": {"seeds": seeds, "sigma": sig, "windows_compared": int(ok.sum()),
+                        "ratio_mc_over_propagated_u": {"p25": q[0, 0], "median": q[1, 0], "p75": q[2, 0]},
+                        "ratio_mc_over_propagated_v": {"p25": q[0, 1], "median": q[1, 1], "p75": q[2, 1]},
+                        "median_sigma_u_px": float(np.median(pred[ok, 0])),
+                        "median_sigma_v_px": float(np.median(pred[ok, 1]))},
+        "data": "synthetic (seeded float32 particle images, config 5)"}), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -644,10 +755,12 @@ def main():
                     help="timed steps (default 1000 for pair, 20 for batch)")
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pair", choices=["pair", "batch", "sweep"],
+    ap.add_argument("--workload", default="pair", choices=["pair", "batch", "sweep", "adjoint"],
                     help="pair: one 4096^2 pair, 32 px windows at step 8 (default); "
                          "batch: 48 pairs of mixed sizes through the 64/32/16 px schedule; "
-                         "sweep: accuracy of every precision against the FP64 pass")
+                         "sweep: accuracy of every precision against the FP64 pass; "
+                         "adjoint: d(u, v)/d(pixels) and propagated uncertainty (config 5)")
+    ap.add_argument("--mc-seeds", type=int, default=1000, help="Monte Carlo seeds of the adjoint workload")
     ap.add_argument("--sweep-size", type=int, default=2048,
                     help="image size of the precision sweep")
     args = ap.parse_args()
@@ -660,6 +773,8 @@ def main():
         run_batch(args)
     elif args.workload == "sweep":
         run_sweep(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

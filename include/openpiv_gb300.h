@@ -178,6 +178,27 @@ int opiv_plan_status(opiv_plan* plan);
  * pedestals (n_win doubles).  Null pointers switch the output off. */
 int opiv_plan_set_plane_output(opiv_plan* plan, float* d_planes, double* d_pedestals);
 
+/* ---- adjoint: d(u, v) / d(pixels) --------------------------------------------
+ * No counterpart in the reference.  For a pair and the peak codes of a
+ * pass over it (the d_out_peak of opiv_process_pair_device; complex or
+ * pocket modes, single-pass plans), the vector u = W/2 - px - fx,
+ * v = W/2 - py - fy depends on the pixels only through the 3-point fit of
+ * five plane values, each a direct correlation sum; the adjoint recomputes
+ * them (no plane is stored) and
+ *  - with d_cotangent (n_win x 2 floats: dL/du, dL/dv per window) adds the
+ *    vector-Jacobian product into d_grad_a / d_grad_b (float images of the
+ *    frames' size, grad_pitch_bytes per row; accumulated, not cleared);
+ *  - with d_sigma (n_win x 2 floats) writes the propagated standard
+ *    deviation of u and v for independent pixel noise of variance var_a
+ *    (frame A) and var_b (frame B); NaN where the fit takes the log of a
+ *    non-positive value, 0 for windows without two peaks.
+ * Integer peaks are held fixed (their derivative is zero almost everywhere).
+ * Asynchronous on `stream`. */
+int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_t pitch_bytes,
+                      const int32_t* d_peak, const float* d_cotangent, float* d_grad_a,
+                      float* d_grad_b, size_t grad_pitch_bytes, float var_a, float var_b,
+                      float* d_sigma, void* stream);
+
 /* ---- multi-pass window offsetting ------------------------------------------
  * No counterpart in the reference (its README lists multi-pass as to do,
  * README.md:280); composed from the reference's per-window steps.  Pass 0 is

@@ -914,6 +914,38 @@ int opiv_batch_results(opiv_batch* b, int pair, int pass, opiv_vector* out_vec, 
     return opiv_multipass_results(b->pairs[pair], pass, out_vec, out_peak, out_disp);
 }
 
+int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_t pitch_bytes,
+                      const int32_t* d_peak, const float* d_cotangent, float* d_grad_a,
+                      float* d_grad_b, size_t grad_pitch_bytes, float var_a, float var_b,
+                      float* d_sigma, void* stream)
+{
+    if (!plan || !d_fa || !d_fb || !d_peak) return fail(OPIV_ERR_ARG, "null argument");
+    if (d_cotangent && (!d_grad_a || !d_grad_b))
+        return fail(OPIV_ERR_ARG, "a cotangent needs both gradient images");
+    if (d_cotangent && (grad_pitch_bytes % sizeof(float) != 0 ||
+                        grad_pitch_bytes < sizeof(float) * plan->img_w))
+        return fail(OPIV_ERR_ARG, "gradient pitch %zu too small or not a multiple of 4", grad_pitch_bytes);
+    if (plan->mode != OPIV_CORR_COMPLEX)
+        return fail(OPIV_ERR_UNSUPPORTED, "the adjoint covers the complex-type modes");
+    if (pitch_bytes < (size_t)plan->img_w * px_bytes(plan->dtype) ||
+        pitch_bytes % px_bytes(plan->dtype) != 0)
+        return fail(OPIV_ERR_ARG, "pitch %zu too small or not a multiple of the pixel size", pitch_bytes);
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(plan->device);
+    PivParams k = base_params(plan);
+    k.fa = d_fa;
+    k.fb = d_fb;
+    k.pitch = pitch_bytes;
+    const cudaError_t e = launch_piv_adjoint(k, (int)plan->ia, plan->dtype, d_peak, d_cotangent,
+                                             d_grad_a, d_grad_b, grad_pitch_bytes / sizeof(float),
+                                             var_a, var_b, d_sigma, (cudaStream_t)stream);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(e, "opiv_plan_adjoint");
+    ++g_launches;
+    return OPIV_OK;
+}
+
 int opiv_plan_set_precision(opiv_plan* plan, int precision)
 {
     if (!plan) return fail(OPIV_ERR_ARG, "plan is null");

@@ -55,7 +55,7 @@ SYMBOLS = [
     "opiv_multipass_results", "opiv_batch_create", "opiv_batch_destroy", "opiv_batch_frames",
     "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
     "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
-    "opiv_process_pairs",
+    "opiv_process_pairs", "opiv_plan_adjoint",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -109,6 +109,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_plan_exact_count.argtypes = [C.c_void_p]
     L.opiv_plan_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.opiv_plan_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_float,
+                                    C.c_float, C.c_void_p, C.c_void_p]
     L.opiv_process_pairs.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p),
                                      C.POINTER(C.c_void_p), C.c_size_t, C.POINTER(C.c_void_p),
                                      C.POINTER(C.c_void_p)]
@@ -273,6 +276,14 @@ class Plan:
                                 fr[0][0].strides[0] if fr else 0,
                                 [v.ctypes.data for v, _ in outs], [p.ctypes.data for _, p in outs])
         return outs
+
+    def adjoint_device(self, d_a: int, d_b: int, pitch: int, d_peak: int, d_cot: int = 0,
+                       d_grad_a: int = 0, d_grad_b: int = 0, grad_pitch: int = 0,
+                       var_a: float = 0.0, var_b: float = 0.0, d_sigma: int = 0, stream: int = 0):
+        """Device pointers: see opiv_plan_adjoint."""
+        _check(load().opiv_plan_adjoint(self._h, d_a, d_b, pitch, d_peak, d_cot or None,
+                                        d_grad_a or None, d_grad_b or None, grad_pitch, var_a, var_b,
+                                        d_sigma or None, stream or None))
 
     def set_precision(self, precision: int):
         """PREC_FP32 (default, reference-exact peaks), PREC_TC_SPLIT_BF16,

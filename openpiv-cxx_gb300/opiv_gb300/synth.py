@@ -143,8 +143,9 @@ def config4(variant: str = "base", size: int = 4096):
                          seed=SEED_BASE + 1000 * 4 + k, full_scale=4095.0)
 
 
-def config5(pair: int = 0, size: int = 2048):
-    """2048^2 float32 in [0, 1], ppp 0.02, I0 ~ U(0.6, 1), sigma 0.02, shift (0.40, 0.25)."""
-    return particle_pair(size, size, ppp=0.02, i0_range=(0.6, 1.0), noise=0.02,
+def config5(pair: int = 0, size: int = 2048, noise: float = 0.02):
+    """2048^2 float32 in [0, 1], ppp 0.02, I0 ~ U(0.6, 1), sigma 0.02, shift
+    (0.40, 0.25).  noise = 0 gives the clean pair (Monte Carlo adds its own)."""
+    return particle_pair(size, size, ppp=0.02, i0_range=(0.6, 1.0), noise=noise,
                          displacement=lambda x, y: (np.full_like(x, 0.40), np.full_like(y, 0.25)),
                          dtype=np.float32, seed=SEED_BASE + 1000 * 5 + pair, full_scale=1.0)
