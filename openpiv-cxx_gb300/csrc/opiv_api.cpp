@@ -158,6 +158,9 @@ struct opiv_plan {
     // and a download stream, and the events that order them with the passes
     bool pipe = false;
     cudaStream_t up = nullptr, down = nullptr;
+    cudaStream_t cs2 = nullptr;                 // second compute stream (slot 1)
+    unsigned int* p_flag_count[2] = { nullptr, nullptr };
+    int32_t* p_flag_list[2] = { nullptr, nullptr };
     void* p_fa[2] = { nullptr, nullptr };
     void* p_fb[2] = { nullptr, nullptr };
     opiv_vector* p_vec[2] = { nullptr, nullptr };
@@ -205,8 +208,14 @@ void plan_free(opiv_plan* p)
         if (p->ev_done[k]) cudaEventDestroy(p->ev_done[k]);
         if (p->ev_down[k]) cudaEventDestroy(p->ev_down[k]);
     }
+    if (p->cs2) cudaStreamSynchronize(p->cs2);
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(p->p_flag_count[k]);
+        cudaFree(p->p_flag_list[k]);
+    }
     if (p->up) cudaStreamDestroy(p->up);
     if (p->down) cudaStreamDestroy(p->down);
+    if (p->cs2) cudaStreamDestroy(p->cs2);
     if (p->h_flag_count) cudaFreeHost(p->h_flag_count);
     for (cudaEvent_t& e : p->ev)
         if (e) cudaEventDestroy(e);
@@ -237,10 +246,17 @@ PivParams base_params(const opiv_plan* p)
 // One pass: FP32 kernel over all windows, then the exact pass over the
 // flagged ones.  Two kernel launches.  `prev` (may be null): the previous
 // pass of a multi-pass chain, whose integer displacements offset frame B.
+// flag_count / flag_list: the exact pass's scratch (null: the plan's own;
+// passes that may run concurrently need their own).
 int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_vector* vec,
-             int32_t* peak, cudaStream_t s, const opiv_plan* prev = nullptr)
+             int32_t* peak, cudaStream_t s, const opiv_plan* prev = nullptr,
+             unsigned int* flag_count = nullptr, int32_t* flag_list = nullptr)
 {
     PivParams k = base_params(p);
+    if (flag_count) {
+        k.flag_count = flag_count;
+        k.flag_list = flag_list;
+    }
     k.fa = fa;
     k.fb = fb;
     k.pitch = pitch;
@@ -257,7 +273,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.pgny = (int)prev->g.yc;
         k.pw = (int)prev->ia;
     }
-    CUDA_TRY(cudaMemsetAsync(p->d_flag_count, 0, sizeof(unsigned int), s));
+    CUDA_TRY(cudaMemsetAsync(k.flag_count, 0, sizeof(unsigned int), s));
     if (is_tc(p->precision)) {
         if (((uintptr_t)fa | (uintptr_t)fb | (uintptr_t)pitch) % 16 != 0)
             return fail(OPIV_ERR_ARG, "the tensor-core path needs 16-byte aligned frame rows");
@@ -538,20 +554,32 @@ int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* fram
             if ((e = cudaMalloc(&plan->p_peak[k], sizeof(int32_t) * plan->n_win)) != cudaSuccess) break;
             if ((e = cudaEventCreateWithFlags(&plan->ev_up[k], cudaEventDisableTiming)) != cudaSuccess) break;
             if ((e = cudaEventCreateWithFlags(&plan->ev_done[k], cudaEventDisableTiming)) != cudaSuccess) break;
-            e = cudaEventCreateWithFlags(&plan->ev_down[k], cudaEventDisableTiming);
+            if ((e = cudaEventCreateWithFlags(&plan->ev_down[k], cudaEventDisableTiming)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&plan->p_flag_count[k], sizeof(unsigned int))) != cudaSuccess) break;
+            e = cudaMalloc(&plan->p_flag_list[k], sizeof(int32_t) * plan->n_win);
         }
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->up, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->down, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&plan->cs2, cudaStreamNonBlocking);
         if (e != cudaSuccess) return done(cuda_fail(e, "opiv_process_pairs set-up"));
         plan->pipe = true;
     }
-    // pair i uses slot k = i & 1: its upload waits until pass i-2 has read
-    // the slot's frames, its pass until the download of pair i-2 has read
-    // the slot's outputs; uploads, passes and downloads of neighbouring
-    // pairs overlap
-    cudaStream_t cs = plan->stream;
+    // the plan's timing events cannot follow two streams: off meanwhile
+    const bool timing = plan->timing;
+    plan->timing = false;
+    struct restore_timing {
+        opiv_plan* p;
+        bool t;
+        ~restore_timing() { p->timing = t; }
+    } restore{ plan, timing };
+    // pair i uses slot k = i & 1 and compute stream k: its upload waits
+    // until pass i-2 has read the slot's frames, its pass until the
+    // download of pair i-2 has read the slot's outputs; uploads, passes and
+    // downloads of neighbouring pairs overlap, and so do the exact pass of
+    // one pair (a few SMs) and the FP32 kernel of the next
     for (int64_t i = 0; i < n_pairs; ++i) {
         const int k = (int)(i & 1);
+        cudaStream_t cs = k ? plan->cs2 : plan->stream;
         if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(plan->up, plan->ev_done[k], 0));
         if ((e = cudaMemcpy2DAsync(plan->p_fa[k], row, frames_a[i], pitch_bytes, row, plan->img_h,
                                    cudaMemcpyHostToDevice, plan->up)) != cudaSuccess ||
@@ -562,7 +590,8 @@ int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* fram
         CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_up[k], 0));
         if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_down[k], 0));
         const int rc = run_pass(plan, plan->p_fa[k], plan->p_fb[k], row, plan->p_vec[k],
-                                out_peak ? plan->p_peak[k] : nullptr, cs);
+                                out_peak ? plan->p_peak[k] : nullptr, cs, nullptr,
+                                plan->p_flag_count[k], plan->p_flag_list[k]);
         if (rc != OPIV_OK) return done(rc);
         CUDA_TRY(cudaEventRecord(plan->ev_done[k], cs));
         CUDA_TRY(cudaStreamWaitEvent(plan->down, plan->ev_done[k], 0));
@@ -575,7 +604,8 @@ int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* fram
         CUDA_TRY(cudaEventRecord(plan->ev_down[k], plan->down));
     }
     if ((e = cudaStreamSynchronize(plan->down)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(cs)) != cudaSuccess)
+        (e = cudaStreamSynchronize(plan->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(plan->cs2)) != cudaSuccess)
         return done(cuda_fail(e, "cudaStreamSynchronize"));
     if (plan->d_status) return done(opiv_plan_status(plan));
     return done(OPIV_OK);
