@@ -192,11 +192,11 @@ def cpu_baseline(a, b, grid, budget_s: float = 15.0):
 
 
 # executed tensor-core FLOPs per 32 x 32 window of the DFT-GEMM kernel
-# (vertical tiles of 4 windows): per tile and operand pass, products of
-# M = 128, K = 16 with N = 32 (stage 1: 2, stage 4: 2) and N = 64 (stages 2
-# and 3: 4 each), 2 M N K FLOPs each; split BF16 runs 3 passes (hi*hi,
-# hi*lo, lo*hi)
-TC_FLOP_PER_WINDOW_PASS = 2 * 128 * 16 * (2 * 32 + 4 * 64 + 4 * 64 + 2 * 32) / 4
+# (vertical tiles of 4 windows): per tile and operand pass, 2 M N K FLOPs
+# with K = 16 for stage 1 (two products of M x N = 128 x 32), stage 2 (four
+# of 128 x 64), stage 3 (four of 64 x 64) and stage 4 (two of 128 x 32);
+# split BF16 runs 3 passes (hi*hi, hi*lo, lo*hi)
+TC_FLOP_PER_WINDOW_PASS = 2 * 16 * (2 * 128 * 32 + 4 * 128 * 64 + 4 * 64 * 64 + 2 * 128 * 32) / 4
 
 
 def accuracy(vec, pk, ref_vec, ref_pk):
@@ -371,7 +371,7 @@ def run_ours(args):
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": achieved / bf16_peak, "traffic": None,
                      "kernel": "piv_tc_kernel<split,COMPLEX,u16>", "kernel_ms": statistics.mean(tc_ms),
-                     "flop": "executed MMA FLOPs: 3 passes x (4 N=32 + 8 N=64 products of M=128, K=16) per 4 windows",
+                     "flop": "executed MMA FLOPs: 3 passes x (2 128x32 + 4 128x64 + 4 64x64 + 2 128x32 products, K=16) per 4 windows",
                      "peak_source": "bf16_tflops of MEASURED_PEAKS.json (cuBLAS burst, of measured)",
                      "hbm_gbs_achieved": (2 * IMG * IMG * 2 + N_WIN * 24) / tc_s / 1e9,
                      "hbm_gbs_peak": peaks.get("hbm_gbs")},
