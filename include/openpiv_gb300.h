@@ -125,8 +125,9 @@ int64_t opiv_plan_exact_count(opiv_plan* plan);
 
 /* Many image pairs of the plan's size through opiv_process_pair's pass,
  * pipelined: the upload of pair i+1 and the download of pair i-1 overlap
- * the pass over pair i (two device slots, an upload and a download
- * stream; frames in pinned host memory are needed for the overlap).  No
+ * the pass over pair i (three device slots, two compute streams, an upload
+ * and a download stream; frames in pinned host memory are needed for the
+ * overlap).  No
  * counterpart in the reference (its loop handles one pair).  Returns when
  * every pair's vectors (and peak codes if out_peak is not null) are in host
  * memory. */

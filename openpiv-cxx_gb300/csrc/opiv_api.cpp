@@ -154,19 +154,20 @@ struct opiv_plan {
     int* d_status = nullptr;            // tensor-core wait status
     float* d_planes = nullptr;          // optional plane output (tensor-core precisions)
     double* d_peds = nullptr;
-    // opiv_process_pairs: two slots of device frames and outputs, an upload
-    // and a download stream, and the events that order them with the passes
+    // opiv_process_pairs: kPipeSlots slots of device frames, outputs and
+    // exact-pass scratch, an upload and a download stream, a second compute
+    // stream, and the events that order them with the passes
+    static constexpr int kPipeSlots = 3;
     bool pipe = false;
     cudaStream_t up = nullptr, down = nullptr;
-    cudaStream_t cs2 = nullptr;                 // second compute stream (slot 1)
-    unsigned int* p_flag_count[2] = { nullptr, nullptr };
-    int32_t* p_flag_list[2] = { nullptr, nullptr };
-    void* p_fa[2] = { nullptr, nullptr };
-    void* p_fb[2] = { nullptr, nullptr };
-    opiv_vector* p_vec[2] = { nullptr, nullptr };
-    int32_t* p_peak[2] = { nullptr, nullptr };
-    cudaEvent_t ev_up[2] = { nullptr, nullptr }, ev_done[2] = { nullptr, nullptr },
-                ev_down[2] = { nullptr, nullptr };
+    cudaStream_t cs2 = nullptr;                 // compute stream of odd pairs
+    unsigned int* p_flag_count[kPipeSlots] = {};
+    int32_t* p_flag_list[kPipeSlots] = {};
+    void* p_fa[kPipeSlots] = {};
+    void* p_fb[kPipeSlots] = {};
+    opiv_vector* p_vec[kPipeSlots] = {};
+    int32_t* p_peak[kPipeSlots] = {};
+    cudaEvent_t ev_up[kPipeSlots] = {}, ev_done[kPipeSlots] = {}, ev_down[kPipeSlots] = {};
 };
 
 // A chain of plans over the same image pair: pass k's frame-B windows are
@@ -199,7 +200,7 @@ void plan_free(opiv_plan* p)
     cudaFree(p->d_status);
     if (p->up) cudaStreamSynchronize(p->up);
     if (p->down) cudaStreamSynchronize(p->down);
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < opiv_plan::kPipeSlots; ++k) {
         cudaFree(p->p_fa[k]);
         cudaFree(p->p_fb[k]);
         cudaFree(p->p_vec[k]);
@@ -209,7 +210,7 @@ void plan_free(opiv_plan* p)
         if (p->ev_down[k]) cudaEventDestroy(p->ev_down[k]);
     }
     if (p->cs2) cudaStreamSynchronize(p->cs2);
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < opiv_plan::kPipeSlots; ++k) {
         cudaFree(p->p_flag_count[k]);
         cudaFree(p->p_flag_list[k]);
     }
@@ -547,7 +548,7 @@ int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* fram
     auto done = [&](int st) { cudaSetDevice(prev); return st; };
     cudaError_t e = cudaSuccess;
     if (!plan->pipe) {
-        for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+        for (int k = 0; k < opiv_plan::kPipeSlots && e == cudaSuccess; ++k) {
             if ((e = cudaMalloc(&plan->p_fa[k], row * plan->img_h)) != cudaSuccess) break;
             if ((e = cudaMalloc(&plan->p_fb[k], row * plan->img_h)) != cudaSuccess) break;
             if ((e = cudaMalloc(&plan->p_vec[k], sizeof(opiv_vector) * plan->n_win)) != cudaSuccess) break;
@@ -572,15 +573,17 @@ int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* fram
         bool t;
         ~restore_timing() { p->timing = t; }
     } restore{ plan, timing };
-    // pair i uses slot k = i & 1 and compute stream k: its upload waits
-    // until pass i-2 has read the slot's frames, its pass until the
-    // download of pair i-2 has read the slot's outputs; uploads, passes and
+    // pair i uses slot k = i % 3 and compute stream i % 2: its upload
+    // waits until pass i-3 has read the slot's frames, its pass until the
+    // download of pair i-3 has read the slot's outputs; uploads, passes and
     // downloads of neighbouring pairs overlap, and so do the exact pass of
-    // one pair (a few SMs) and the FP32 kernel of the next
+    // one pair (a few SMs) and the FP32 kernel of the next.  Three slots:
+    // a slot's upload does not wait for the pass just before it.
+    constexpr int S = opiv_plan::kPipeSlots;
     for (int64_t i = 0; i < n_pairs; ++i) {
-        const int k = (int)(i & 1);
-        cudaStream_t cs = k ? plan->cs2 : plan->stream;
-        if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(plan->up, plan->ev_done[k], 0));
+        const int k = (int)(i % S);
+        cudaStream_t cs = (i & 1) ? plan->cs2 : plan->stream;
+        if (i >= S) CUDA_TRY(cudaStreamWaitEvent(plan->up, plan->ev_done[k], 0));
         if ((e = cudaMemcpy2DAsync(plan->p_fa[k], row, frames_a[i], pitch_bytes, row, plan->img_h,
                                    cudaMemcpyHostToDevice, plan->up)) != cudaSuccess ||
             (e = cudaMemcpy2DAsync(plan->p_fb[k], row, frames_b[i], pitch_bytes, row, plan->img_h,
@@ -588,7 +591,7 @@ int opiv_process_pairs(opiv_plan* plan, int64_t n_pairs, const void* const* fram
             return done(cuda_fail(e, "cudaMemcpy2DAsync(frames)"));
         CUDA_TRY(cudaEventRecord(plan->ev_up[k], plan->up));
         CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_up[k], 0));
-        if (i >= 2) CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_down[k], 0));
+        if (i >= S) CUDA_TRY(cudaStreamWaitEvent(cs, plan->ev_down[k], 0));
         const int rc = run_pass(plan, plan->p_fa[k], plan->p_fb[k], row, plan->p_vec[k],
                                 out_peak ? plan->p_peak[k] : nullptr, cs, nullptr,
                                 plan->p_flag_count[k], plan->p_flag_list[k]);
