@@ -148,21 +148,28 @@ piv_w64_kernel(const PivParams p)
     }
     float e0 = 0.f, e1 = 0.f;
     double sa0 = 0.0, sb0 = 0.0, sa1 = 0.0, sb1 = 0.0;
+    // pixels widen straight to float (exact for 8/16-bit frames); doubles
+    // only for the per-window API's exact pedestal (PLANES, double frames)
     for (int i = t; i < N; i += kThreads) {
         const int y = i >> 6, x = i & 63;
-        const double a0 = (double)__ldg(fa + (size_t)(by0 + y) * pitch + bx0 + x);
-        const double b0 = (double)__ldg(fb + (size_t)(by0 + oy0 + y) * pitch + bx0 + ox0 + x);
-        double a1 = 0.0, b1 = 0.0;
+        const PixT pa0 = __ldg(fa + (size_t)(by0 + y) * pitch + bx0 + x);
+        const PixT pb0 = __ldg(fb + (size_t)(by0 + oy0 + y) * pitch + bx0 + ox0 + x);
+        PixT pa1 = PixT(0), pb1 = PixT(0);
         if (valid1) {
-            a1 = (double)__ldg(fa + (size_t)(by1 + y) * pitch + bx1 + x);
-            b1 = (double)__ldg(fb + (size_t)(by1 + oy1 + y) * pitch + bx1 + ox1 + x);
+            pa1 = __ldg(fa + (size_t)(by1 + y) * pitch + bx1 + x);
+            pb1 = __ldg(fb + (size_t)(by1 + oy1 + y) * pitch + bx1 + ox1 + x);
         }
-        const float2 z0 = make_float2((float)a0, (float)b0), z1 = make_float2((float)a1, (float)b1);
+        const float2 z0 = make_float2((float)pa0, (float)pb0), z1 = make_float2((float)pa1, (float)pb1);
         T1[y * LD + x] = z0;
         T2[y * LD + x] = z1;
         e0 = fmaf(z0.x, z0.x, fmaf(z0.y, z0.y, e0));
         e1 = fmaf(z1.x, z1.x, fmaf(z1.y, z1.y, e1));
-        if (PLANES) { sa0 += a0; sb0 += b0; sa1 += a1; sb1 += b1; }
+        if (PLANES) {
+            sa0 += (double)pa0;
+            sb0 += (double)pb0;
+            sa1 += (double)pa1;
+            sb1 += (double)pb1;
+        }
     }
     e0 = block_sum(e0, red);
     e1 = block_sum(e1, red);
