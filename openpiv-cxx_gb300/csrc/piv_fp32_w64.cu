@@ -2,11 +2,15 @@
 //
 // A 64-point row does not fit one lane's registers next to everything else,
 // so this kernel keeps the pair's spectra in shared memory: one CTA of 256
-// threads per pair of windows, two padded 64 x 65 float2 tiles.  The steps
+// threads per pair of windows, two padded 64 x 67 float2 tiles.  The steps
 // and the formulas are those of the 16/32 kernel (piv_fp32.cuh):
 //   z = a + i b; 2-D FFT (rows, then columns) as radix-4 decimation-in-
 //   frequency passes over the tile (64 = 4^3; outputs in base-4 digit-
 //   reversed order, absorbed in the indexing);
+//   bank-conflict-free tile layout: column c of a row sits at c + c/16 and
+//   rows are 67 float2 apart, so sixteen threads reading sixteen
+//   neighbouring rows, sixteen neighbouring columns, or the sixteen columns
+//   of a digit-reversed block all hit distinct banks;
 //   4 conj(P) = (2 Im(Z Zm), |Z|^2 - |Zm|^2) with Zm = Z[-k] (P = B conj A,
 //   fft.h:188-227), REAL mode's zeroed spectrum row 0, row W/2, column 0
 //   (fft.h:166-183), DC product dropped and the pedestal added back;
@@ -28,7 +32,7 @@ namespace w64 {
 
 constexpr int W = 64;
 constexpr int N = W * W;
-constexpr int LD = W + 1;            // padded row stride (float2)
+constexpr int LD = W + 3;            // row stride (float2), odd: rows fall on distinct banks
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr float kFitTol = 3e-5f;
@@ -43,22 +47,24 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 w)
     return make_float2(fmaf(a.x, w.x, -a.y * w.y), fmaf(a.x, w.y, a.y * w.x));
 }
 
-// Forward radix-4 DIF over all 64 lines of tile T; rows when `rows`, else
-// columns.  tw[k] = exp(-2 pi i k / 64).  Each line ends in base-4 digit-
-// reversed order.
-__device__ void dif4_lines(float2* T, bool rows, const float2* tw)
+// offset of column c inside a row: one pad element after every 16 columns
+__device__ __forceinline__ int pos(int c) { return c + (c >> 4); }
+
+// Forward radix-4 DIF over all 64 lines of tile T (rows when ROWS, else
+// columns).  tw[k] = exp(-2 pi i k / 64).  Each line ends in base-4 digit-
+// reversed order.  Neighbouring threads take neighbouring lines and the
+// same butterfly, so a warp's twiddles are one broadcast.
+template <bool ROWS>
+__device__ void dif4_lines(float2* T, const float2* tw)
 {
-    const int es = rows ? 1 : LD, ls = rows ? LD : 1;
     for (int q = 16; q >= 1; q >>= 2) {
         for (int k = threadIdx.x; k < 64 * 16; k += kThreads) {
-            // rows: neighbouring threads walk along a line; columns: across lines
-            const int line = rows ? (k >> 4) : (k & 63);
-            const int b = rows ? (k & 15) : (k >> 6);
+            const int line = k & 63, b = k >> 6;
             const int j = b % q;
             const int base = (b / q) * 4 * q + j;
-            float2* x = T + line * ls;
-            const float2 a = x[base * es], bb = x[(base + q) * es];
-            const float2 c = x[(base + 2 * q) * es], d = x[(base + 3 * q) * es];
+            auto el = [&](int e) -> float2& { return ROWS ? T[line * LD + pos(e)] : T[e * LD + pos(line)]; };
+            const float2 a = el(base), bb = el(base + q);
+            const float2 c = el(base + 2 * q), d = el(base + 3 * q);
             const float2 t0 = make_float2(a.x + c.x, a.y + c.y), t1 = make_float2(a.x - c.x, a.y - c.y);
             const float2 t2 = make_float2(bb.x + d.x, bb.y + d.y), t3 = make_float2(bb.x - d.x, bb.y - d.y);
             // length-4 DFT, forward: y1 = t1 - i t3, y3 = t1 + i t3
@@ -67,10 +73,10 @@ __device__ void dif4_lines(float2* T, bool rows, const float2* tw)
             const float2 y1 = make_float2(t1.x + t3.y, t1.y - t3.x);
             const float2 y3 = make_float2(t1.x - t3.y, t1.y + t3.x);
             const int s = 16 / q;   // W_{4q}^{j m} = tw[j m 64 / (4q)]
-            x[base * es] = y0;
-            x[(base + q) * es] = cmul(y1, tw[(j * s) & 63]);
-            x[(base + 2 * q) * es] = cmul(y2, tw[(2 * j * s) & 63]);
-            x[(base + 3 * q) * es] = cmul(y3, tw[(3 * j * s) & 63]);
+            el(base) = y0;
+            el(base + q) = cmul(y1, tw[(j * s) & 63]);
+            el(base + 2 * q) = cmul(y2, tw[(2 * j * s) & 63]);
+            el(base + 3 * q) = cmul(y3, tw[(3 * j * s) & 63]);
         }
         __syncthreads();
     }
@@ -78,12 +84,12 @@ __device__ void dif4_lines(float2* T, bool rows, const float2* tw)
 
 __device__ __forceinline__ void fft2d(float2* T, const float2* tw)
 {
-    dif4_lines(T, true, tw);
-    dif4_lines(T, false, tw);
+    dif4_lines<true>(T, tw);
+    dif4_lines<false>(T, tw);
 }
 
 // position in a transformed tile of spectrum bin (ky, kx) / plane (y, x)
-__device__ __forceinline__ int at(int r, int c) { return dr(r) * LD + dr(c); }
+__device__ __forceinline__ int at(int r, int c) { return dr(r) * LD + pos(dr(c)); }
 
 __device__ __forceinline__ void window_origin(const PivParams& p, int w, int& bx, int& by)
 {
@@ -160,8 +166,8 @@ piv_w64_kernel(const PivParams p)
             pb1 = __ldg(fb + (size_t)(by1 + oy1 + y) * pitch + bx1 + ox1 + x);
         }
         const float2 z0 = make_float2((float)pa0, (float)pb0), z1 = make_float2((float)pa1, (float)pb1);
-        T1[y * LD + x] = z0;
-        T2[y * LD + x] = z1;
+        T1[y * LD + pos(x)] = z0;
+        T2[y * LD + pos(x)] = z1;
         e0 = fmaf(z0.x, z0.x, fmaf(z0.y, z0.y, e0));
         e1 = fmaf(z1.x, z1.x, fmaf(z1.y, z1.y, e1));
         if (PLANES) {
@@ -235,7 +241,7 @@ piv_w64_kernel(const PivParams p)
 #pragma unroll
     for (int n = 0; n < N / kThreads; ++n) {
         const int i = t + n * kThreads;
-        T1[(i >> 6) * LD + (i & 63)] = q[n];
+        T1[(i >> 6) * LD + pos(i & 63)] = q[n];
     }
     __syncthreads();
     fft2d(T1, tw);   // T1[at(y, x)] = plane1(y, x) + i plane2(y, x), 4x scaled
