@@ -4,11 +4,11 @@
 // so this kernel keeps the pair's spectra in shared memory: one CTA of 256
 // threads per pair of windows, two padded 64 x 67 float2 tiles.  The steps
 // and the formulas are those of the 16/32 kernel (piv_fp32.cuh):
-//   z = a + i b; 2-D FFT (rows, then columns) as radix-4 decimation-in-
-//   frequency passes over the tile (64 = 4^3; outputs in base-4 digit-
+//   z = a + i b; 2-D FFT (rows, then columns) as two radix-8 decimation-
+//   in-frequency passes over the tile (64 = 8^2; outputs in base-8 digit-
 //   reversed order, absorbed in the indexing);
-//   bank-conflict-free tile layout: column c of a row sits at c + c/16 and
-//   rows are 67 float2 apart, so sixteen threads reading sixteen
+//   bank-conflict-free tile layout: column c of a row sits at c + 2 (c/16)
+//   and rows are 71 float2 apart, so sixteen threads reading sixteen
 //   neighbouring rows, sixteen neighbouring columns, or the sixteen columns
 //   of a digit-reversed block all hit distinct banks;
 //   4 conj(P) = (2 Im(Z Zm), |Z|^2 - |Zm|^2) with Zm = Z[-k] (P = B conj A,
@@ -32,60 +32,85 @@ namespace w64 {
 
 constexpr int W = 64;
 constexpr int N = W * W;
-constexpr int LD = W + 3;            // row stride (float2), odd: rows fall on distinct banks
+constexpr int LD = W + 7;            // row stride (float2), odd: rows fall on distinct banks
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr float kFitTol = 3e-5f;
 constexpr float kSnTol = 3e-6f;
 #define kNegInf64 (-__int_as_float(0x7f800000))
 
-// base-4 digit reversal of a 6-bit index (an involution)
-__device__ __forceinline__ int dr(int v) { return ((v & 3) << 4) | (v & 12) | (v >> 4); }
+// base-8 digit reversal of a 6-bit index (an involution)
+__device__ __forceinline__ int dr(int v) { return ((v & 7) << 3) | (v >> 3); }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 w)
 {
     return make_float2(fmaf(a.x, w.x, -a.y * w.y), fmaf(a.x, w.y, a.y * w.x));
 }
 
-// offset of column c inside a row: one pad element after every 16 columns
-__device__ __forceinline__ int pos(int c) { return c + (c >> 4); }
+// offset of column c inside a row: two pad elements after every 16 columns
+__device__ __forceinline__ int pos(int c) { return c + 2 * (c >> 4); }
 
-// Forward radix-4 DIF over all 64 lines of tile T (rows when ROWS, else
-// columns).  tw[k] = exp(-2 pi i k / 64).  Each line ends in base-4 digit-
-// reversed order.  Neighbouring threads take neighbouring lines and the
-// same butterfly, so a warp's twiddles are one broadcast.
-template <bool ROWS>
-__device__ void dif4_lines(float2* T, const float2* tw)
+// In-place forward 8-point DFT, natural order in and out.
+__device__ __forceinline__ void dft8(float2* x)
 {
-    for (int q = 16; q >= 1; q >>= 2) {
-        for (int k = threadIdx.x; k < 64 * 16; k += kThreads) {
-            const int line = k & 63, b = k >> 6;
-            const int j = b % q;
-            const int base = (b / q) * 4 * q + j;
-            auto el = [&](int e) -> float2& { return ROWS ? T[line * LD + pos(e)] : T[e * LD + pos(line)]; };
-            const float2 a = el(base), bb = el(base + q);
-            const float2 c = el(base + 2 * q), d = el(base + 3 * q);
-            const float2 t0 = make_float2(a.x + c.x, a.y + c.y), t1 = make_float2(a.x - c.x, a.y - c.y);
-            const float2 t2 = make_float2(bb.x + d.x, bb.y + d.y), t3 = make_float2(bb.x - d.x, bb.y - d.y);
-            // length-4 DFT, forward: y1 = t1 - i t3, y3 = t1 + i t3
-            const float2 y0 = make_float2(t0.x + t2.x, t0.y + t2.y);
-            const float2 y2 = make_float2(t0.x - t2.x, t0.y - t2.y);
-            const float2 y1 = make_float2(t1.x + t3.y, t1.y - t3.x);
-            const float2 y3 = make_float2(t1.x - t3.y, t1.y + t3.x);
-            const int s = 16 / q;   // W_{4q}^{j m} = tw[j m 64 / (4q)]
-            el(base) = y0;
-            el(base + q) = cmul(y1, tw[(j * s) & 63]);
-            el(base + 2 * q) = cmul(y2, tw[(2 * j * s) & 63]);
-            el(base + 3 * q) = cmul(y3, tw[(3 * j * s) & 63]);
+    constexpr float r = 0.70710678118654752f;   // cos(pi/4)
+    const float2 a0 = make_float2(x[0].x + x[4].x, x[0].y + x[4].y), a1 = make_float2(x[0].x - x[4].x, x[0].y - x[4].y);
+    const float2 a2 = make_float2(x[2].x + x[6].x, x[2].y + x[6].y), a3 = make_float2(x[2].x - x[6].x, x[2].y - x[6].y);
+    const float2 a4 = make_float2(x[1].x + x[5].x, x[1].y + x[5].y), a5 = make_float2(x[1].x - x[5].x, x[1].y - x[5].y);
+    const float2 a6 = make_float2(x[3].x + x[7].x, x[3].y + x[7].y), a7 = make_float2(x[3].x - x[7].x, x[3].y - x[7].y);
+    // even outputs: 4-point DFT of (a0, a4, a2, a6)
+    const float2 e0 = make_float2(a0.x + a2.x, a0.y + a2.y), e1 = make_float2(a0.x - a2.x, a0.y - a2.y);
+    const float2 e2 = make_float2(a4.x + a6.x, a4.y + a6.y), e3 = make_float2(a4.x - a6.x, a4.y - a6.y);
+    x[0] = make_float2(e0.x + e2.x, e0.y + e2.y);
+    x[4] = make_float2(e0.x - e2.x, e0.y - e2.y);
+    x[2] = make_float2(e1.x + e3.y, e1.y - e3.x);   // e1 - i e3
+    x[6] = make_float2(e1.x - e3.y, e1.y + e3.x);   // e1 + i e3
+    // odd outputs: 4-point DFT of (a1, a5 w, -i a3, a7 w^3), w = exp(-i pi/4)
+    const float2 b1 = make_float2((a5.x + a5.y) * r, (a5.y - a5.x) * r);
+    const float2 b3 = make_float2((a7.y - a7.x) * r, -(a7.x + a7.y) * r);
+    const float2 o0 = make_float2(a1.x + a3.y, a1.y - a3.x), o1 = make_float2(a1.x - a3.y, a1.y + a3.x);
+    const float2 o2 = make_float2(b1.x + b3.x, b1.y + b3.y), o3 = make_float2(b1.x - b3.x, b1.y - b3.y);
+    x[1] = make_float2(o0.x + o2.x, o0.y + o2.y);
+    x[5] = make_float2(o0.x - o2.x, o0.y - o2.y);
+    x[3] = make_float2(o1.x + o3.y, o1.y - o3.x);   // o1 - i o3
+    x[7] = make_float2(o1.x - o3.y, o1.y + o3.x);   // o1 + i o3
+}
+
+// One radix-8 DIF pass over all 64 lines of tile T (rows when ROWS, else
+// columns).  FIRST: butterfly j takes elements j + 8 m and scales output m
+// by tw[j m] = exp(-2 pi i j m / 64); second pass: butterfly j takes
+// elements 8 j + m, no twiddles.  After both passes bin k0 + 8 k1 of a line
+// sits at 8 k0 + k1.  Neighbouring threads take neighbouring lines and the
+// same butterfly, so a warp's twiddles are one broadcast.
+template <bool ROWS, bool FIRST>
+__device__ __forceinline__ void dif8_pass(float2* T, const float2* tw)
+{
+#pragma unroll
+    for (int it = 0; it < 64 * 8 / kThreads; ++it) {
+        const int k = (int)threadIdx.x + it * kThreads;
+        const int line = k & 63, j = k >> 6;
+        const int base = FIRST ? j : 8 * j, es = FIRST ? 8 : 1;
+        auto el = [&](int e) -> float2& { return ROWS ? T[line * LD + pos(e)] : T[e * LD + pos(line)]; };
+        float2 x[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) x[m] = el(base + m * es);
+        dft8(x);
+        if (FIRST) {
+#pragma unroll
+            for (int m = 1; m < 8; ++m) x[m] = cmul(x[m], tw[j * m]);
         }
-        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < 8; ++m) el(base + m * es) = x[m];
     }
+    __syncthreads();
 }
 
 __device__ __forceinline__ void fft2d(float2* T, const float2* tw)
 {
-    dif4_lines<true>(T, tw);
-    dif4_lines<false>(T, tw);
+    dif8_pass<true, true>(T, tw);
+    dif8_pass<true, false>(T, tw);
+    dif8_pass<false, true>(T, tw);
+    dif8_pass<false, false>(T, tw);
 }
 
 // position in a transformed tile of spectrum bin (ky, kx) / plane (y, x)
@@ -102,6 +127,27 @@ __device__ __forceinline__ void window_origin(const PivParams& p, int w, int& bx
         by = p.gy0 + gy * p.gdy;
     }
 }
+
+// Running top-2 of strict 4-neighbour maxima (find_peaks) plus the largest
+// value whose strict-maximum decision is within dlt of flipping.
+struct Top2 {
+    float t0, t1, umax;
+    int key;
+    __device__ __forceinline__ void init()
+    {
+        t0 = t1 = umax = kNegInf64;
+        key = 0x7fffffff;
+    }
+    __device__ __forceinline__ void add(float c, float m, float dlt, int k)
+    {
+        const float dd = m - c;
+        if (fabsf(dd) <= dlt) umax = fmaxf(umax, c);
+        if (dd < 0.f) {
+            if (c > t0) { t1 = t0; t0 = c; key = k; }
+            else t1 = fmaxf(t1, c);
+        }
+    }
+};
 
 __device__ __forceinline__ float block_sum(float v, float* red)
 {
@@ -249,6 +295,34 @@ piv_w64_kernel(const PivParams p)
     const float dlt = p.kappa * 5.9604645e-8f * 2.f * (float)N * (e0 + e1);
     const int lane = t & 31, wp = t >> 5;
 
+    // ---- find_peaks on both planes at once: thread = (column, 16-row
+    // block); rows roll through registers, the horizontal neighbours come
+    // from the neighbouring lanes (the two edge lanes read theirs)
+    Top2 s0, s1;
+    s0.init();
+    s1.init();
+    {
+        const int xs = t & 63, yb = (t >> 6) * 16;
+        const bool col_ok = xs >= SX0 && xs < SX1;
+        auto cell = [&](int ys, int x) -> float2 {   // swapped-plane values of both planes
+            return T1[at((ys + W / 2) & (W - 1), (x + W / 2) & (W - 1))];
+        };
+        float2 up = cell(yb - 1, xs), cc = cell(yb, xs);
+        for (int ys = yb; ys < yb + 16; ++ys) {
+            const float2 dn = cell(ys + 1, xs);
+            float2 lf = make_float2(__shfl_up_sync(0xffffffffu, cc.x, 1), __shfl_up_sync(0xffffffffu, cc.y, 1));
+            float2 rt = make_float2(__shfl_down_sync(0xffffffffu, cc.x, 1), __shfl_down_sync(0xffffffffu, cc.y, 1));
+            if (lane == 0) lf = cell(ys, xs - 1);
+            if (lane == 31) rt = cell(ys, xs + 1);
+            if (col_ok && ys >= SY0 && ys < SY1) {
+                s0.add(cc.x, fmaxf(fmaxf(up.x, dn.x), fmaxf(lf.x, rt.x)), dlt, ys * W + xs);
+                s1.add(cc.y, fmaxf(fmaxf(up.y, dn.y), fmaxf(lf.y, rt.y)), dlt, ys * W + xs);
+            }
+            up = cc;
+            cc = dn;
+        }
+    }
+
     for (int h = 0; h < 2; ++h) {
         const int w = h ? w1 : w0;
         const bool valid = h ? valid1 : true;
@@ -261,23 +335,8 @@ piv_w64_kernel(const PivParams p)
             for (int i = t; i < N; i += kThreads)
                 p.planes[(size_t)w * N + i] = 0.25f * val(i >> 6, i & 63);
 
-        // ---- find_peaks: thread = (column, 16-row block), then block reduce
-        const int xs = t & 63, yb = (t >> 6) * 16;
-        const bool col_ok = xs >= SX0 && xs < SX1;
-        float t0 = kNegInf64, t1 = kNegInf64, umax = kNegInf64;
-        int key = 0x7fffffff;
-        for (int ys = yb; ys < yb + 16; ++ys) {
-            if (!(col_ok && ys >= SY0 && ys < SY1)) continue;
-            const float c = val(ys, xs);
-            const float m = fmaxf(fmaxf(val(ys - 1, xs), val(ys + 1, xs)),
-                                  fmaxf(val(ys, xs - 1), val(ys, xs + 1)));
-            const float dd = m - c;
-            if (fabsf(dd) <= dlt) umax = fmaxf(umax, c);
-            if (dd < 0.f) {
-                if (c > t0) { t1 = t0; t0 = c; key = ys * W + xs; }
-                else t1 = fmaxf(t1, c);
-            }
-        }
+        float t0 = h ? s1.t0 : s0.t0, t1 = h ? s1.t1 : s0.t1, umax = h ? s1.umax : s0.umax;
+        int key = h ? s1.key : s0.key;
         // warp reduction (ties to the lowest row-major index)
         for (int o = 16; o > 0; o >>= 1) {
             const float o0 = __shfl_xor_sync(0xffffffffu, t0, o);
