@@ -123,6 +123,56 @@ __device__ __forceinline__ void load_row(const PixT* ptr, float2 (&v)[W])
     }
 }
 
+// A row that starts anywhere (B windows shifted by a previous pass's
+// displacement): the 16-byte blocks covering it are loaded whole and the
+// row is shifted out of them by the start's offset inside its block (a
+// word select, then a byte permute).  The blocks read hold at least one
+// pixel of the row each, so they lie inside the frame's allocation.
+template <int W, bool B, typename PixT>
+__device__ __forceinline__ void load_row_shifted(const PixT* ptr, float2 (&v)[W])
+{
+    if constexpr (sizeof(PixT) > 4) {   // double frames: element loads
+#pragma unroll
+        for (int x = 0; x < W; ++x) put<B>(v[bitrev<W>(x)], (float)__ldg(ptr + x));
+    } else {
+        constexpr int NW = W * (int)sizeof(PixT) / 4;   // 32-bit words of the row
+        constexpr int NC = NW / 4;                      // whole blocks of the row
+        const uintptr_t a = reinterpret_cast<uintptr_t>(ptr);
+        const uint4* q = reinterpret_cast<const uint4*>(a & ~(uintptr_t)15);
+        const int mis = (int)(a & 15);
+        uint32_t w[NW + 4];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const uint4 r = __ldg(q + c);
+            w[4 * c] = r.x; w[4 * c + 1] = r.y; w[4 * c + 2] = r.z; w[4 * c + 3] = r.w;
+        }
+        uint4 tail = make_uint4(0u, 0u, 0u, 0u);
+        if (mis != 0) tail = __ldg(q + NC);   // only a misaligned row reaches into it
+        w[NW] = tail.x; w[NW + 1] = tail.y; w[NW + 2] = tail.z; w[NW + 3] = tail.w;
+        const int ws = mis >> 2;
+        const uint32_t sel = 0x3210u + 0x1111u * (uint32_t)(mis & 3);
+#pragma unroll
+        for (int k = 0; k < NW + 2; ++k) w[k] = (ws & 2) ? w[k + 2] : w[k];
+#pragma unroll
+        for (int k = 0; k < NW + 1; ++k) w[k] = (ws & 1) ? w[k + 1] : w[k];
+#pragma unroll
+        for (int k = 0; k < NW; ++k) {
+            const uint32_t u = __byte_perm(w[k], w[k + 1], sel);
+            if constexpr (sizeof(PixT) == 2) {
+                put<B>(v[bitrev<W>(2 * k)], u16_lo(u));
+                put<B>(v[bitrev<W>(2 * k + 1)], u16_hi(u));
+            } else if constexpr (sizeof(PixT) == 1) {
+                put<B>(v[bitrev<W>(4 * k + 0)], u8_k<0>(u));
+                put<B>(v[bitrev<W>(4 * k + 1)], u8_k<1>(u));
+                put<B>(v[bitrev<W>(4 * k + 2)], u8_k<2>(u));
+                put<B>(v[bitrev<W>(4 * k + 3)], u8_k<3>(u));
+            } else {
+                put<B>(v[bitrev<W>(k)], __uint_as_float(u));
+            }
+        }
+    }
+}
+
 // Bottom-left corner of window w.  Window indices fit in 32 bits (plans
 // hold at most 2^31 - 1 windows), so the grid position is a 32-bit division.
 __device__ __forceinline__ void window_origin(const PivParams& p, int w, int& bx, int& by)
@@ -214,7 +264,7 @@ piv_fp32_kernel(const PivParams p)
                 const size_t off = (size_t)(by + gl) * pitch + bx;
                 load_row<W, false, PixT, VEC>(fa + off, v);
                 if (p.prev_disp != nullptr)   // shifted B rows need not be aligned
-                    load_row<W, true, PixT, false>(fb + (size_t)(by + oy + gl) * pitch + bx + ox, v);
+                    load_row_shifted<W, true, PixT>(fb + (size_t)(by + oy + gl) * pitch + bx + ox, v);
                 else
                     load_row<W, true, PixT, VEC>(fb + off, v);
                 if (PLANES) {   // exact pedestal for the per-window API (double input)
