@@ -253,6 +253,16 @@ int opiv_batch_run(opiv_batch* batch, int use_graph, void* stream);
 int64_t opiv_batch_window_count(const opiv_batch* batch, int pair, int pass);
 int opiv_batch_results(opiv_batch* batch, int pair, int pass, opiv_vector* out_vec,
                        int32_t* out_peak, int32_t* out_disp);
+/* Host frames in, every pair's final-pass vectors out, pipelined: pair i's
+ * frames go up on an upload stream, its pass chain starts on a fork stream
+ * as soon as they are in, and its vectors (and peak codes when out_peak is
+ * not null) come back on a download stream as soon as its last pass ends,
+ * so copies overlap the other pairs' passes (frames and outputs in pinned
+ * host memory are needed for the overlap).  pitch_bytes: one row pitch per
+ * pair.  Returns when every pair's results are in host memory. */
+int opiv_batch_process(opiv_batch* batch, const void* const* frames_a, const void* const* frames_b,
+                       const size_t* pitch_bytes, opiv_vector* const* out_vec,
+                       int32_t* const* out_peak);
 
 /* ---- allocation-free pass ------------------------------------------------ */
 /* No counterpart in the reference.  The same pass as opiv_process_pair_device

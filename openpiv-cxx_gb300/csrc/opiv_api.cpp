@@ -50,6 +50,13 @@ int cuda_fail(cudaError_t e, const char* what)
         if (e_ != cudaSuccess) return cuda_fail(e_, #call);     \
     } while (0)
 
+// the same inside functions that restore the caller's device through `done`
+#define CUDA_TRY_D(call)                                              \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) return done(cuda_fail(e_, #call));     \
+    } while (0)
+
 // openpiv/core/util.h:67-70
 bool is_pow2(uint64_t v) { return v && (v == (v & (~v + 1))); }
 
@@ -768,6 +775,9 @@ struct opiv_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int device = 0;
+    // opiv_batch_process: copy streams and one upload / done event per pair
+    cudaStream_t up = nullptr, down = nullptr;
+    std::vector<cudaEvent_t> ev_up, ev_done;
 };
 
 int opiv_batch_destroy(opiv_batch* b)
@@ -781,7 +791,11 @@ int opiv_batch_destroy(opiv_batch* b)
     if (b->main) cudaStreamSynchronize(b->main);
     for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
     if (b->main) cudaStreamDestroy(b->main);
+    if (b->up) cudaStreamDestroy(b->up);
+    if (b->down) cudaStreamDestroy(b->down);
     for (cudaEvent_t ev : b->events) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : b->ev_up) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : b->ev_done) cudaEventDestroy(ev);
     for (void* f : b->d_fa) cudaFree(f);
     for (void* f : b->d_fb) cudaFree(f);
     cudaSetDevice(prev);
@@ -931,6 +945,73 @@ int opiv_batch_run(opiv_batch* b, int use_graph, void* stream)
     }
     if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return done(cuda_fail(e, "cudaGraphLaunch"));
     g_launches += 2 * (int64_t)b->pairs.size() * (int64_t)b->pairs[0]->passes.size();
+    return done(OPIV_OK);
+}
+
+int opiv_batch_process(opiv_batch* b, const void* const* frames_a, const void* const* frames_b,
+                       const size_t* pitch_bytes, opiv_vector* const* out_vec, int32_t* const* out_peak)
+{
+    if (!b || !frames_a || !frames_b || !pitch_bytes || !out_vec) return fail(OPIV_ERR_ARG, "null argument");
+    const int n = (int)b->pairs.size();
+    for (int i = 0; i < n; ++i) {
+        const opiv_plan* p0 = b->pairs[i]->passes[0];
+        if (!frames_a[i] || !frames_b[i] || !out_vec[i] || (out_peak && !out_peak[i]))
+            return fail(OPIV_ERR_ARG, "null buffer for pair %d", i);
+        if (pitch_bytes[i] < (size_t)p0->img_w * px_bytes(p0->dtype))
+            return fail(OPIV_ERR_ARG, "pitch %zu of pair %d smaller than a row", pitch_bytes[i], i);
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaError_t e = cudaSuccess;
+    if (!b->up) {
+        if ((e = cudaStreamCreateWithFlags(&b->up, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaStreamCreateWithFlags(&b->down, cudaStreamNonBlocking)) != cudaSuccess)
+            return done(cuda_fail(e, "cudaStreamCreateWithFlags"));
+        for (int i = 0; i < n; ++i) {
+            cudaEvent_t eu, ed;
+            if ((e = cudaEventCreateWithFlags(&eu, cudaEventDisableTiming)) != cudaSuccess)
+                return done(cuda_fail(e, "cudaEventCreateWithFlags"));
+            b->ev_up.push_back(eu);
+            if ((e = cudaEventCreateWithFlags(&ed, cudaEventDisableTiming)) != cudaSuccess)
+                return done(cuda_fail(e, "cudaEventCreateWithFlags"));
+            b->ev_done.push_back(ed);
+        }
+    }
+    // work already queued on the batch's stream comes first
+    const int ns = (int)b->streams.size();
+    CUDA_TRY_D(cudaEventRecord(b->events[ns], b->main));
+    CUDA_TRY_D(cudaStreamWaitEvent(b->up, b->events[ns], 0));
+    for (int i = 0; i < ns; ++i) CUDA_TRY_D(cudaStreamWaitEvent(b->streams[i], b->events[ns], 0));
+    for (int i = 0; i < n; ++i) {
+        const opiv_plan* p0 = b->pairs[i]->passes[0];
+        const size_t row = (size_t)p0->img_w * px_bytes(p0->dtype);
+        CUDA_TRY_D(cudaMemcpy2DAsync(b->d_fa[i], b->pitch[i], frames_a[i], pitch_bytes[i], row, p0->img_h,
+                                     cudaMemcpyHostToDevice, b->up));
+        CUDA_TRY_D(cudaMemcpy2DAsync(b->d_fb[i], b->pitch[i], frames_b[i], pitch_bytes[i], row, p0->img_h,
+                                     cudaMemcpyHostToDevice, b->up));
+        CUDA_TRY_D(cudaEventRecord(b->ev_up[i], b->up));
+    }
+    for (int i = 0; i < n; ++i) {
+        cudaStream_t cs = b->streams[i % ns];
+        CUDA_TRY_D(cudaStreamWaitEvent(cs, b->ev_up[i], 0));
+        const int rc = opiv_multipass_process_device(b->pairs[i], b->d_fa[i], b->d_fb[i], b->pitch[i], cs);
+        if (rc != OPIV_OK) {
+            cudaDeviceSynchronize();
+            return done(rc);
+        }
+        CUDA_TRY_D(cudaEventRecord(b->ev_done[i], cs));
+        const opiv_plan* pl = b->pairs[i]->passes.back();
+        CUDA_TRY_D(cudaStreamWaitEvent(b->down, b->ev_done[i], 0));
+        CUDA_TRY_D(cudaMemcpyAsync(out_vec[i], pl->d_vec, sizeof(opiv_vector) * pl->n_win,
+                                   cudaMemcpyDeviceToHost, b->down));
+        if (out_peak)
+            CUDA_TRY_D(cudaMemcpyAsync(out_peak[i], pl->d_peak, sizeof(int32_t) * pl->n_win,
+                                       cudaMemcpyDeviceToHost, b->down));
+    }
+    if ((e = cudaStreamSynchronize(b->down)) != cudaSuccess) return done(cuda_fail(e, "cudaStreamSynchronize"));
+    // the fork streams have finished too (every pair's download waited on them)
     return done(OPIV_OK);
 }
 

@@ -55,7 +55,7 @@ SYMBOLS = [
     "opiv_multipass_results", "opiv_batch_create", "opiv_batch_destroy", "opiv_batch_frames",
     "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
     "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
-    "opiv_process_pairs", "opiv_plan_adjoint",
+    "opiv_process_pairs", "opiv_plan_adjoint", "opiv_batch_process",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -154,6 +154,8 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_batch_window_count.argtypes = [C.c_void_p, C.c_int, C.c_int]
     L.opiv_batch_results.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                      C.c_void_p]
+    L.opiv_batch_process.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                     C.POINTER(C.c_size_t), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -411,6 +413,31 @@ class Batch:
 
     def run(self, use_graph: bool = True, stream: int = 0):
         _check(load().opiv_batch_run(self._h, int(bool(use_graph)), stream or None))
+
+    def process_into(self, ptrs_a, ptrs_b, pitches, ptrs_vec, ptrs_peak=None):
+        """Host pointers, one per pair (pinned for overlap): every pair's
+        upload, passes and final-pass download, pipelined (opiv_batch_process)."""
+        n = len(self.sizes)
+        arr = lambda xs: (C.c_void_p * n)(*xs)
+        _check(load().opiv_batch_process(self._h, arr(ptrs_a), arr(ptrs_b), (C.c_size_t * n)(*pitches),
+                                         arr(ptrs_vec), arr(ptrs_peak) if ptrs_peak is not None else None))
+
+    def process(self, frames):
+        """[(frame_a, frame_b), ...] numpy frames, one per pair -> [(final-pass
+        vectors, peak codes), ...]."""
+        if len(frames) != len(self.sizes):
+            raise OpivError(ERR_ARG, f"{len(frames)} pairs for a batch of {len(self.sizes)}")
+        fr = [(np.ascontiguousarray(a, self.dtype), np.ascontiguousarray(b, self.dtype)) for a, b in frames]
+        for (a, b), (w, h) in zip(fr, self.sizes):
+            if a.shape != (h, w) or b.shape != (h, w):
+                raise OpivError(ERR_SIZE_MISMATCH, f"image size is different from expected: {a.shape}")
+        last = len(self.passes) - 1
+        outs = [(np.zeros((self.window_count(i, last), 5), np.float32),
+                 np.zeros(self.window_count(i, last), np.int32)) for i in range(len(fr))]
+        self.process_into([a.ctypes.data for a, _ in fr], [b.ctypes.data for _, b in fr],
+                          [a.strides[0] for a, _ in fr], [v.ctypes.data for v, _ in outs],
+                          [p.ctypes.data for _, p in outs])
+        return outs
 
     def window_count(self, pair: int, k: int) -> int:
         return int(load().opiv_batch_window_count(self._h, pair, k))

@@ -366,6 +366,32 @@ def test_batch_graph_matches_per_pair_multipass():
         check(j, f"replay {j}")
     assert og.kernel_launch_count() - before == 4 * 2 * len(sizes) * len(passes)
     assert batch.window_count(2, 2) == 127 * 127
+    # the pipelined host call: same final-pass results, frames of both sets,
+    # one of them behind a padded row pitch
+    for j in (0, 1, 0):
+        fr = [frames[2 * i + j] for i in range(len(sizes))]
+        if j == 1:
+            padded = np.zeros((sizes[0][1], sizes[0][0] + 24), np.uint16)
+            pb = padded.copy()
+            padded[:, :sizes[0][0]], pb[:, :sizes[0][0]] = fr[0]
+            fr[0] = (padded[:, :sizes[0][0]], pb[:, :sizes[0][0]])
+        before = og.kernel_launch_count()
+        if j == 1:   # non-contiguous views reach the C call with their own pitch
+            last = len(passes) - 1
+            outs = [(np.zeros((batch.window_count(i, last), 5), np.float32),
+                     np.zeros(batch.window_count(i, last), np.int32)) for i in range(len(sizes))]
+            batch.process_into([a.ctypes.data for a, _ in fr], [b.ctypes.data for _, b in fr],
+                               [a.strides[0] for a, _ in fr], [v.ctypes.data for v, _ in outs],
+                               [p.ctypes.data for _, p in outs])
+        else:
+            outs = batch.process(fr)
+        assert og.kernel_launch_count() - before == 2 * len(sizes) * len(passes)
+        for i, (vec, pk) in enumerate(outs):
+            ref = expect[i][j][len(passes) - 1]
+            assert np.array_equal(vec, ref[0]), f"process {j}: pair {i} vectors differ"
+            assert np.array_equal(pk, ref[1]), f"process {j}: pair {i} peaks differ"
+    with pytest.raises(og.OpivError):
+        batch.process(frames[:2])
     batch.close()
 
 
