@@ -565,12 +565,56 @@ def run_batch(args):
 
 
 # ---- precision sweep -----------------------------------------------------------
+def fp64_numpy_pass(a, b, grid, ia, img_h, chunk=2048):
+    """Vectors and peak codes of the reference's chain on numpy FP64
+    correlation planes, for window sizes the FP64 GPU pass does not take
+    (48 px: not a power of two).  Complex mode: IFFT(FFT(b) conj FFT(a)),
+    unnormalised, quadrant-swapped (fft.h:188-206); find_peaks(plane, 2, 1):
+    strict 4-neighbour maxima over rows [1, W-2), columns [1, W-1), the two
+    largest (ties: lower row-major index) (image_utils.impl.h:42-74); the
+    3-point Gaussian fit (impl:77-101); the vector of main.cpp:220-236."""
+    n = len(grid)
+    vec = np.zeros((n, 5), np.float64)
+    pk = np.full(n, -1, np.int64)
+    for s0 in range(0, n, chunk):
+        g = grid[s0:s0 + chunk]
+        wa = np.stack([a[y:y + ia, x:x + ia] for x, y in g]).astype(np.float64)
+        wb = np.stack([b[y:y + ia, x:x + ia] for x, y in g]).astype(np.float64)
+        r = np.fft.ifft2(np.fft.fft2(wb) * np.conj(np.fft.fft2(wa))).real * (ia * ia)
+        pl = np.fft.fftshift(r, axes=(1, 2))
+        c = pl[:, 1:ia - 2, 1:ia - 1]
+        strict = ((c > pl[:, 0:ia - 3, 1:ia - 1]) & (c > pl[:, 2:ia - 1, 1:ia - 1]) &
+                  (c > pl[:, 1:ia - 2, 0:ia - 2]) & (c > pl[:, 1:ia - 2, 2:ia]))
+        cand = np.where(strict, c, -np.inf).reshape(len(g), -1)
+        order = np.argsort(-cand, axis=1, kind="stable")[:, :2]
+        v0 = np.take_along_axis(cand, order[:, :1], 1)[:, 0]
+        v1 = np.take_along_axis(cand, order[:, 1:2], 1)[:, 0]
+        ok = np.isfinite(v1)
+        cw = ia - 2
+        py, px = order[:, 0] // cw + 1, order[:, 0] % cw + 1
+        idx = np.arange(len(g))
+        C, L, R = pl[idx, py, px], pl[idx, py, px - 1], pl[idx, py, px + 1]
+        U, D = pl[idx, py - 1, px], pl[idx, py + 1, px]
+        with np.errstate(all="ignore"):
+            fx = np.where((L > 0) & (C > 0) & (R > 0),
+                          (np.log(L) - np.log(R)) / (2 * (np.log(L) + np.log(R) - 2 * np.log(C))), np.nan)
+            fy = np.where((U > 0) & (C > 0) & (D > 0),
+                          (np.log(U) - np.log(D)) / (2 * (np.log(U) + np.log(D) - 2 * np.log(C))), np.nan)
+            sn = np.where(v1 > 0, v0 / v1, 0.0)
+        out = np.stack([g[:, 0] + ia // 2, img_h - (g[:, 1] + ia // 2), ia // 2 - px - fx,
+                        ia // 2 - py - fy, sn], axis=1)
+        vec[s0:s0 + chunk] = np.where(ok[:, None], out, 0.0)
+        pk[s0:s0 + chunk] = np.where(ok, py * ia + px, -1)
+    return vec, pk
+
+
 def run_sweep(args):
-    """Displacement error of every precision against the FP64 pass on the
-    config-2 field: windows 16 / 32 / 64 px at 75 % overlap, at config-2
-    statistics, low seeding (0.005 ppp) and high noise (sigma 80).  The
-    tensor-core precisions cover 32 px windows; 48 px windows are not a
-    power of two, which the reference's FFT rejects (fft.h:76-84)."""
+    """Displacement error of every precision against the FP64 reference on
+    the config-2 field: windows 16 / 32 / 48 / 64 px at 75 % overlap, at
+    config-2 statistics, low seeding (0.005 ppp) and high noise (sigma 80).
+    The FP64 reference is the FP64 GPU pass for powers of two and numpy
+    FP64 planes through the reference's peak search and fit for 48 px, which
+    the reference's FFT rejects (fft.h:76-84): no FP32-FFT row there."""
     import torch
 
     import opiv_gb300 as og
@@ -584,17 +628,23 @@ def run_sweep(args):
     rows = []
     for variant in ("base", "sparse", "noisy"):
         a, b = synth.config4(variant, size)
-        for ia in (16, 32, 64):
+        for ia in (16, 32, 48, 64):
             step = ia // 4
 
             def plan(prec):
+                if ia == 48:
+                    return og.Plan(size, size, np.uint16, ia, step, mode=og.CORR_COMPLEX, tensor_core=prec)
                 p = og.Plan(size, size, np.uint16, ia, step, mode=og.CORR_COMPLEX)
                 p.set_precision(prec)
                 return p
 
-            ref_vec, ref_pk = plan(og.PREC_FP64).process(a, b)
+            if ia == 48:
+                ref_vec, ref_pk = fp64_numpy_pass(a, b, og.grid_offsets(size, size, ia, ia, step, step),
+                                                  ia, size)
+            else:
+                ref_vec, ref_pk = plan(og.PREC_FP64).process(a, b)
             for name, prec in precisions:
-                if prec != og.PREC_FP32 and ia != 32:
+                if prec == og.PREC_FP32 and ia == 48:
                     continue
                 p = plan(prec)
                 vec, pk = p.process(a, b)
@@ -605,7 +655,7 @@ def run_sweep(args):
                 rows.append({"variant": variant, "ia": ia, "step": step, "precision": name,
                              "windows": p.n, "kernel_ms": ms,
                              **accuracy(vec, pk, ref_vec, ref_pk)})
-    print(json.dumps({"metric": "precision sweep vs FP64 pass", "size": size,
+    print(json.dumps({"metric": "precision sweep vs FP64 reference", "size": size,
                       "data": "synthetic config-2 field (seeded particle images, 12-bit)",
                       "rows": rows}), flush=True)
 

@@ -147,12 +147,13 @@ int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
  * No counterpart in the reference (it computes in double only).
  * OPIV_PREC_FP32 (default): the FP32 kernels plus the exact re-decision
  *   pass; integer peaks identical to the reference, u, v within 1e-4 px.
- * OPIV_PREC_TC_SPLIT_BF16: 32 x 32 windows as four DFT matrix products on
- *   the tensor cores, BF16 operands split into hi + lo parts, FP32
- *   accumulation; no exact pass (a window whose top two plane values lie
- *   within the rounding may pick the other peak).  Needs u8/u16 frames,
- *   window x positions and x step multiples of 8 pixels, 16-byte aligned
- *   rows; OPIV_ERR_UNSUPPORTED otherwise.
+ * OPIV_PREC_TC_SPLIT_BF16: 16, 32, 48 or 64 px windows as four DFT matrix
+ *   products on the tensor cores, BF16 operands split into hi + lo parts,
+ *   FP32 accumulation; no exact pass (a window whose top two plane values
+ *   lie within the rounding may pick the other peak).  Needs u8/u16 frames
+ *   and 16-byte aligned rows; 32 px windows also window x positions and x
+ *   step multiples of 8 pixels; OPIV_ERR_UNSUPPORTED otherwise.  48 px windows need a plan from
+ *   opiv_plan_create_tc (the FFT path takes powers of 2 only).
  * OPIV_PREC_TC_BF16: the same with plain BF16 operands (one MMA per product).
  * OPIV_PREC_TC_SPLIT_FP16 / OPIV_PREC_TC_FP16: the same with FP16 operands
  *   (11-bit significand), kept inside FP16's range by powers of two (a
@@ -170,6 +171,16 @@ enum {
     OPIV_PREC_TC_FP16 = 5
 };
 int opiv_plan_set_precision(opiv_plan* plan, int precision);
+
+/* A plan of the tensor-core path alone, created with one of the
+ * OPIV_PREC_TC_* precisions: 16, 32, 48 or 64 px windows.  A DFT matrix
+ * needs no power of 2, so 48 px windows, which FFT::FFT rejects
+ * (fft.h:76-84, OPIV_ERR_NOT_POW2 from opiv_plan_create), are taken here;
+ * such a plan refuses OPIV_PREC_FP32 / OPIV_PREC_FP64 and the adjoint with
+ * OPIV_ERR_NOT_POW2.  Other arguments as opiv_plan_create. */
+int opiv_plan_create_tc(opiv_plan** plan, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
+                        uint32_t dx, uint32_t dy, int mode, int limit_search, int precision,
+                        int device);
 /* OPIV_OK, or OPIV_ERR_TIMEOUT if a tensor-core pass of this plan gave up
  * waiting for its MMAs since the last call (waits for the plan's work). */
 int opiv_plan_status(opiv_plan* plan);

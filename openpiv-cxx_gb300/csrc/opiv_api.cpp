@@ -289,7 +289,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.planes = p->d_planes;
         k.peds = p->d_peds;
         if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
-        CUDA_TRY(launch_piv_tc(k, p->dtype, p->mode, p->limit,
+        CUDA_TRY(launch_piv_tc(k, (int)p->ia, p->dtype, p->mode, p->limit,
                                p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_SPLIT_FP16,
                                p->precision == OPIV_PREC_TC_SPLIT_FP16 || p->precision == OPIV_PREC_TC_FP16,
                                p->d_tc, s));
@@ -381,8 +381,12 @@ int64_t opiv_grid(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_t ia_h,
                              (uint32_t)(ia_h * step_fraction), out_xy, cap);
 }
 
-int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
-                     uint32_t dx, uint32_t dy, int mode, int limit_search, int device)
+namespace {
+
+// tc_only: a plan of the tensor-core path alone (any window size that path
+// takes, powers of 2 or not); otherwise the FFT path's rules
+int plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia, uint32_t dx,
+                uint32_t dy, int mode, int limit_search, int device, bool tc_only)
 {
     if (out == nullptr) return fail(OPIV_ERR_ARG, "plan pointer is null");
     *out = nullptr;
@@ -393,9 +397,15 @@ int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype,
     grid_geom g;
     int rc = grid_geometry(img_w, img_h, ia, ia, dx, dy, g);
     if (rc != OPIV_OK) return rc;
-    if (!is_pow2(ia)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", ia, ia);
-    if (!fp32_supports((int)ia) || !exact_supports((int)ia))
-        return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", ia, ia);
+    if (tc_only) {
+        if (!tc_supports((int)ia, dtype))
+            return fail(OPIV_ERR_UNSUPPORTED,
+                        "the tensor-core path takes 16, 32, 48 or 64 px windows of u8/u16 frames");
+    } else {
+        if (!is_pow2(ia)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", ia, ia);
+        if (!fp32_supports((int)ia) || !exact_supports((int)ia))
+            return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", ia, ia);
+    }
     if (g.xs + (int64_t)dx * (g.xc - 1) + ia > (int64_t)img_w || g.ys + (int64_t)dy * (g.yc - 1) + ia > (int64_t)img_h)
         return fail(OPIV_ERR_RECT_OUTSIDE, "extract: rectangle to extract is too large for image");
 
@@ -443,14 +453,42 @@ int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype,
     if ((e = cudaMallocHost(&p->h_flag_count, sizeof(unsigned int))) != cudaSuccess)
         return done(cuda_fail(e, "cudaMallocHost"));
     *p->h_flag_count = 0;
-    std::vector<double2> tw = reference_twiddles(ia, -1), tr = reference_twiddles(ia, +1);
-    tw.insert(tw.end(), tr.begin(), tr.end());
-    if ((e = cudaMalloc(&p->d_tw, sizeof(double2) * tw.size())) != cudaSuccess)
-        return done(cuda_fail(e, "cudaMalloc(twiddles)"));
-    if ((e = cudaMemcpy(p->d_tw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice)) !=
-        cudaSuccess)
-        return done(cuda_fail(e, "cudaMemcpy(twiddles)"));
+    if (is_pow2(ia)) {   // the exact kernel's twiddles (FFT path)
+        std::vector<double2> tw = reference_twiddles(ia, -1), tr = reference_twiddles(ia, +1);
+        tw.insert(tw.end(), tr.begin(), tr.end());
+        if ((e = cudaMalloc(&p->d_tw, sizeof(double2) * tw.size())) != cudaSuccess)
+            return done(cuda_fail(e, "cudaMalloc(twiddles)"));
+        if ((e = cudaMemcpy(p->d_tw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+            return done(cuda_fail(e, "cudaMemcpy(twiddles)"));
+    }
     return done(OPIV_OK);
+}
+
+}  // namespace
+
+int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
+                     uint32_t dx, uint32_t dy, int mode, int limit_search, int device)
+{
+    return plan_create(out, img_w, img_h, dtype, ia, dx, dy, mode, limit_search, device, false);
+}
+
+int opiv_plan_create_tc(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
+                        uint32_t dx, uint32_t dy, int mode, int limit_search, int precision, int device)
+{
+    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_FP16)
+        return fail(OPIV_ERR_ARG, "unknown precision %d", precision);
+    if (!is_tc(precision)) return fail(OPIV_ERR_ARG, "precision %d is not a tensor-core precision", precision);
+    int rc = plan_create(out, img_w, img_h, dtype, ia, dx, dy, mode, limit_search, device, true);
+    if (rc != OPIV_OK) return rc;
+    rc = opiv_plan_set_precision(*out, precision);
+    if (rc != OPIV_OK) {
+        const std::string msg = opiv_last_error();
+        opiv_plan_destroy(*out);
+        *out = nullptr;
+        return fail(rc, "%s", msg.c_str());
+    }
+    return OPIV_OK;
 }
 
 int opiv_plan_destroy(opiv_plan* plan)
@@ -1041,6 +1079,8 @@ int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_
         return fail(OPIV_ERR_ARG, "gradient pitch %zu too small or not a multiple of 4", grad_pitch_bytes);
     if (plan->mode != OPIV_CORR_COMPLEX)
         return fail(OPIV_ERR_UNSUPPORTED, "the adjoint covers the complex-type modes");
+    if (!is_pow2(plan->ia))
+        return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", plan->ia, plan->ia);
     if (pitch_bytes < (size_t)plan->img_w * px_bytes(plan->dtype) ||
         pitch_bytes % px_bytes(plan->dtype) != 0)
         return fail(OPIV_ERR_ARG, "pitch %zu too small or not a multiple of the pixel size", pitch_bytes);
@@ -1065,19 +1105,21 @@ int opiv_plan_set_precision(opiv_plan* plan, int precision)
     if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
     if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_FP16)
         return fail(OPIV_ERR_ARG, "unknown precision %d", precision);
+    if (!is_tc(precision) && !is_pow2(plan->ia))
+        return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", plan->ia, plan->ia);
     if (is_tc(precision)) {
         if (!tc_supports((int)plan->ia, plan->dtype))
             return fail(OPIV_ERR_UNSUPPORTED,
-                        "the tensor-core path takes 32x32 windows of u8/u16 frames");
-        if (plan->g.xs % 8 != 0 || plan->dx % 8 != 0)
+                        "the tensor-core path takes 16, 32, 48 or 64 px windows of u8/u16 frames");
+        if (plan->ia == 32 && (plan->g.xs % 8 != 0 || plan->dx % 8 != 0))
             return fail(OPIV_ERR_UNSUPPORTED,
-                        "the tensor-core path needs window x positions on multiples of 8 pixels");
+                        "the 32 px tensor-core path needs window x positions on multiples of 8 pixels");
         if (!plan->d_tc) {
             int prev = 0;
             cudaGetDevice(&prev);
             cudaSetDevice(plan->device);
-            std::vector<unsigned char> host(tc_constant_bytes());
-            tc_constants(host.data());
+            std::vector<unsigned char> host(tc_constant_bytes((int)plan->ia));
+            tc_constants((int)plan->ia, host.data());
             cudaError_t e = cudaMalloc(&plan->d_tc, host.size());
             if (e == cudaSuccess)
                 e = cudaMemcpy(plan->d_tc, host.data(), host.size(), cudaMemcpyHostToDevice);

@@ -43,15 +43,16 @@ struct PivParams {
     int* status = nullptr;             // tensor-core kernel: set to 1 if an MMA wait gave up
 };
 
-// Tensor-core DFT-GEMM kernel (piv_tc.cu): 32 x 32 windows, u8/u16 frames,
+// Tensor-core DFT-GEMM kernels (piv_tc.cu): 16, 32, 48 and 64 px windows
+// (32: piv_tc_kernel.cuh; the others: piv_tcg_kernel.cuh), u8/u16 frames,
 // window x positions and steps multiples of 8 pixels.  Constant matrices,
-// each 32 x 32 BF16 in the K-major no-swizzle operand layout, all hi parts
+// each W x W 16-bit in the K-major no-swizzle operand layout, all hi parts
 // then all lo parts; -S, C, S adjacent so that [C; S] and [-S; C] are
-// 64-row operands.
+// 2W-row operands.
 enum { kTcG1 = 0, kTcNS = 1, kTcC = 2, kTcS = 3, kTcC4 = 4, kTcNumMat = 5 };
 bool tc_supports(int w, int dtype);
-size_t tc_constant_bytes();
-void tc_constants(unsigned char* out);
+size_t tc_constant_bytes(int w);
+void tc_constants(int w, unsigned char* out);
 // Adjoint of a pass (piv_adjoint.cu): complex-mode planes, peaks from the
 // forward pass, cotangents (n_win x 2) pulled back into float image
 // gradients (accumulated, gpitch floats per row) and/or the propagated
@@ -60,9 +61,9 @@ cudaError_t launch_piv_adjoint(const PivParams& p, int w, int dtype, const int32
                                const float* cot, float* grad_a, float* grad_b, size_t gpitch,
                                float var_a, float var_b, float* sigma, cudaStream_t s);
 
-// consts: tc_constant_bytes() bytes from tc_constants (BF16 set, FP16 set)
-cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
-                          const void* consts, cudaStream_t s);
+// consts: tc_constant_bytes(w) bytes from tc_constants (BF16 set, FP16 set)
+cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int limit, bool split,
+                          bool fp16, const void* consts, cudaStream_t s);
 
 // Fused FP32 kernels, one entry per window size (piv_fp32_w*.cu; 64 x 64
 // windows use the shared-memory kernel of piv_fp32_w64.cu).  Frames

@@ -1,6 +1,7 @@
-// Host side of the tensor-core kernel (piv_tc_kernel.cuh): the constant
-// matrices in BF16 and FP16 (hi and lo parts, canonical operand layout) and
-// the dispatch to the two instantiation units.
+// Host side of the tensor-core kernels (piv_tc_kernel.cuh for 32 px
+// windows, piv_tcg_kernel.cuh for 16, 48 and 64 px): the constant matrices
+// in BF16 and FP16 (hi and lo parts, canonical operand layout) and the
+// dispatch to the instantiation units.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -14,16 +15,22 @@ cudaError_t launch_piv_tc_bf16(const PivParams& p, int dtype, int mode, int limi
                                const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tc_fp16(const PivParams& p, int dtype, int mode, int limit, bool split,
                                const void* consts, cudaStream_t s);
+cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+                               const void* consts, cudaStream_t s);
+cudaError_t launch_piv_tcg_w48(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+                               const void* consts, cudaStream_t s);
+cudaError_t launch_piv_tcg_w64(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+                               const void* consts, cudaStream_t s);
 
 namespace tc {
 
-constexpr int kMat = 2048;   // one 32 x 32 16-bit matrix
-constexpr int kSetBytes = kTcNumMat * 2 * kMat;
+// bytes of the hi and lo parts of the five W x W 16-bit matrices
+constexpr int set_bytes(int w) { return kTcNumMat * 2 * w * w * 2; }
 
-// byte offset of element (n, k) in a 32 x 32 K-major matrix
-constexpr int kmaj32(int n, int k)
+// byte offset of element (n, k) in a W x W K-major matrix
+constexpr int kmaj(int w, int n, int k)
 {
-    return ((n >> 3) * 4 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2;
+    return ((n >> 3) * (w / 8) + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2;
 }
 
 // BF16: round to nearest even (finite inputs)
@@ -79,17 +86,27 @@ float fp16_value(uint16_t h)
 
 }  // namespace tc
 
-bool tc_supports(int w, int dtype) { return w == 32 && (dtype == kU8 || dtype == kU16); }
+bool tc_supports(int w, int dtype)
+{
+    return (w == 16 || w == 32 || w == 48 || w == 64) && (dtype == kU8 || dtype == kU16);
+}
 
-size_t tc_constant_bytes() { return 2 * (size_t)tc::kSetBytes; }
+size_t tc_constant_bytes(int w) { return 2 * (size_t)tc::set_bytes(w); }
 
 // Two sets: BF16, then FP16 (the FP16 stage-1 matrix scaled by 2^-9).
-void tc_constants(unsigned char* out)
+// Matrix rows n are the products' output index, columns k the summed one:
+//   G1  n < W/2: cos(2 pi n x / W); n = W/2: (-1)^x; n > W/2: sin(2 pi (n - W/2) x / W)
+//   C, S, -S  cos / sin (2 pi n k / W)
+//   C4  n = x' (the swapped column, x = (x' + W/2) mod W), k = (part, k_x):
+//       part 0: 1 (k_x = 0) or 2 cos(2 pi k_x x / W); part 1: (-1)^x (k_x = 0)
+//       or -2 sin(2 pi k_x x / W)
+void tc_constants(int w, unsigned char* out)
 {
     using namespace tc;
     const double pi = 3.14159265358979323846;
+    const int h = w / 2, mat = w * w * 2, sb = set_bytes(w);
     for (int set = 0; set < 2; ++set) {
-        unsigned char* o = out + set * kSetBytes;
+        unsigned char* o = out + set * sb;
         auto put = [&](int m, int n, int k, double v) {
             uint16_t hi, lo;
             if (set == 0) {
@@ -99,39 +116,44 @@ void tc_constants(unsigned char* out)
                 hi = fp16_bits((float)v);
                 lo = fp16_bits((float)(v - (double)fp16_value(hi)));
             }
-            std::memcpy(o + m * kMat + kmaj32(n, k), &hi, 2);
-            std::memcpy(o + (kTcNumMat + m) * kMat + kmaj32(n, k), &lo, 2);
+            std::memcpy(o + m * mat + kmaj(w, n, k), &hi, 2);
+            std::memcpy(o + (kTcNumMat + m) * mat + kmaj(w, n, k), &lo, 2);
         };
         const double gscale = set == 0 ? 1.0 : 1.0 / 512.0;
-        for (int n = 0; n < 32; ++n)
-            for (int k = 0; k < 32; ++k) {
-                // stage 1, B[k = x][n = coefficient]
+        for (int n = 0; n < w; ++n)
+            for (int k = 0; k < w; ++k) {
                 double g;
-                if (n < 16) g = std::cos(2 * pi * n * k / 32.0);
-                else if (n == 16) g = (k & 1) ? -1.0 : 1.0;
-                else g = std::sin(2 * pi * (n - 16) * k / 32.0);
+                if (n < h) g = std::cos(2 * pi * n * k / w);
+                else if (n == h) g = (k & 1) ? -1.0 : 1.0;
+                else g = std::sin(2 * pi * (n - h) * k / w);
                 put(kTcG1, n, k, g * gscale);
-                const double c = std::cos(2 * pi * n * k / 32.0), s = std::sin(2 * pi * n * k / 32.0);
+                const double c = std::cos(2 * pi * n * k / w), s = std::sin(2 * pi * n * k / w);
                 put(kTcC, n, k, c);
                 put(kTcS, n, k, s);
                 put(kTcNS, n, k, -s);
-                // stage 4, B[k = (part, k_x)][n = x'], x = (x' + 16) mod 32
-                const int x = (n + 16) & 31;
-                const int part = k >> 4, kx = k & 15;
+                const int x = (n + h) % w;
+                const int part = k / h, kx = k % h;
                 double v;
-                if (part == 0) v = kx == 0 ? 1.0 : 2.0 * std::cos(2 * pi * kx * x / 32.0);
-                else v = kx == 0 ? ((x & 1) ? -1.0 : 1.0) : -2.0 * std::sin(2 * pi * kx * x / 32.0);
+                if (part == 0) v = kx == 0 ? 1.0 : 2.0 * std::cos(2 * pi * kx * x / w);
+                else v = kx == 0 ? ((x & 1) ? -1.0 : 1.0) : -2.0 * std::sin(2 * pi * kx * x / w);
                 put(kTcC4, n, k, v);
             }
     }
 }
 
-cudaError_t launch_piv_tc(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
-                          const void* consts, cudaStream_t s)
+cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int limit, bool split,
+                          bool fp16, const void* consts, cudaStream_t s)
 {
     const unsigned char* c = static_cast<const unsigned char*>(consts);
-    return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, c + tc::kSetBytes, s)
-                : launch_piv_tc_bf16(p, dtype, mode, limit, split, c, s);
+    const unsigned char* set = c + (fp16 ? tc::set_bytes(w) : 0);
+    switch (w) {
+    case 16: return launch_piv_tcg_w16(p, dtype, mode, limit, split, fp16, set, s);
+    case 32: return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, set, s)
+                         : launch_piv_tc_bf16(p, dtype, mode, limit, split, set, s);
+    case 48: return launch_piv_tcg_w48(p, dtype, mode, limit, split, fp16, set, s);
+    case 64: return launch_piv_tcg_w64(p, dtype, mode, limit, split, fp16, set, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace opiv

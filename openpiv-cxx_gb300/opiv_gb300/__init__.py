@@ -55,7 +55,7 @@ SYMBOLS = [
     "opiv_multipass_results", "opiv_batch_create", "opiv_batch_destroy", "opiv_batch_frames",
     "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
     "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
-    "opiv_process_pairs", "opiv_plan_adjoint", "opiv_batch_process",
+    "opiv_process_pairs", "opiv_plan_adjoint", "opiv_batch_process", "opiv_plan_create_tc",
 ]
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -97,6 +97,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_grid_offsets.argtypes = [C.c_uint32] * 6 + [_ip, C.c_int64]
     L.opiv_plan_create.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_int,
                                    C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_int]
+    L.opiv_plan_create_tc.argtypes = [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_int,
+                                      C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_int,
+                                      C.c_int]
     L.opiv_plan_destroy.argtypes = [C.c_void_p]
     L.opiv_plan_window_count.restype = C.c_int64
     L.opiv_plan_window_count.argtypes = [C.c_void_p]
@@ -199,15 +202,23 @@ class Plan:
     """One image geometry + window size + grid step + correlation mode."""
 
     def __init__(self, img_w: int, img_h: int, dtype, ia: int, dx: int, dy: int | None = None,
-                 mode: int = CORR_COMPLEX, limit_search: bool = False, device: int = 0):
+                 mode: int = CORR_COMPLEX, limit_search: bool = False, device: int = 0,
+                 tensor_core: int | None = None):
+        """tensor_core: one of the PREC_TC_* precisions for a plan of the
+        tensor-core path alone (opiv_plan_create_tc: 16, 32, 48 or 64 px
+        windows, 48 included)."""
         L = load()
         dy = dx if dy is None else dy
         self.dtype = np.dtype(dtype)
         if self.dtype not in DTYPES:
             raise OpivError(ERR_ARG, f"unsupported pixel type {self.dtype}")
         h = C.c_void_p()
-        _check(L.opiv_plan_create(C.byref(h), img_w, img_h, DTYPES[self.dtype], ia, dx, dy, mode,
-                                  int(bool(limit_search)), device))
+        if tensor_core is not None:
+            _check(L.opiv_plan_create_tc(C.byref(h), img_w, img_h, DTYPES[self.dtype], ia, dx, dy, mode,
+                                         int(bool(limit_search)), tensor_core, device))
+        else:
+            _check(L.opiv_plan_create(C.byref(h), img_w, img_h, DTYPES[self.dtype], ia, dx, dy, mode,
+                                      int(bool(limit_search)), device))
         self._h = h
         self.img_w, self.img_h, self.ia, self.dx, self.dy = img_w, img_h, ia, dx, dy
         self.mode, self.limit_search = mode, bool(limit_search)

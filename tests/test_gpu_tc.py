@@ -28,23 +28,36 @@ def _torch():
     return pytest.importorskip("torch")
 
 
-def reference_planes(a, b, grid):
-    """Swapped correlation planes minus the pedestal sum(a) sum(b), FP64."""
-    wa = np.stack([a[y:y + W, x:x + W] for x, y in grid]).astype(np.float64)
-    wb = np.stack([b[y:y + W, x:x + W] for x, y in grid]).astype(np.float64)
-    r = np.fft.ifft2(np.fft.fft2(wb) * np.conj(np.fft.fft2(wa))).real * (W * W)
-    ped = wa.sum((1, 2)) * wb.sum((1, 2))
+def reference_planes(a, b, grid, ia=W, mode=og.CORR_COMPLEX):
+    """Swapped correlation planes minus the pedestal sum(a) sum(b) (REAL
+    mode: the reference's F4 unpacked-out spectrum rows and column zeroed,
+    no pedestal), FP64, any window size."""
+    wa = np.stack([a[y:y + ia, x:x + ia] for x, y in grid]).astype(np.float64)
+    wb = np.stack([b[y:y + ia, x:x + ia] for x, y in grid]).astype(np.float64)
+    fa, fb = np.fft.fft2(wa), np.fft.fft2(wb)
+    if mode == og.CORR_REAL:
+        for f in (fa, fb):
+            f[:, 0, :] = 0
+            f[:, ia // 2, :] = 0
+            f[:, :, 0] = 0
+        ped = np.zeros(len(grid))
+    else:
+        ped = wa.sum((1, 2)) * wb.sum((1, 2))
+    r = np.fft.ifft2(fb * np.conj(fa)).real * (ia * ia)
     return np.fft.fftshift(r, axes=(1, 2)) - ped[:, None, None], ped
 
 
-def run(a, b, step, precision, mode=og.CORR_COMPLEX, limit=False, planes=False):
+def run(a, b, step, precision, mode=og.CORR_COMPLEX, limit=False, planes=False, ia=W):
     torch = _torch()
     h, w = a.shape
-    plan = og.Plan(w, h, a.dtype, W, step, mode=mode, limit_search=limit)
-    plan.set_precision(precision)
+    if ia == 48:   # not a power of 2: a plan of the tensor-core path alone
+        plan = og.Plan(w, h, a.dtype, ia, step, mode=mode, limit_search=limit, tensor_core=precision)
+    else:
+        plan = og.Plan(w, h, a.dtype, ia, step, mode=mode, limit_search=limit)
+        plan.set_precision(precision)
     out = {}
     if planes:
-        dpl = torch.zeros((plan.n, W, W), dtype=torch.float32, device="cuda")
+        dpl = torch.zeros((plan.n, ia, ia), dtype=torch.float32, device="cuda")
         dped = torch.zeros(plan.n, dtype=torch.float64, device="cuda")
         plan.set_plane_output(dpl.data_ptr(), dped.data_ptr())
     vec, pk = plan.process(a, b)
@@ -54,6 +67,26 @@ def run(a, b, step, precision, mode=og.CORR_COMPLEX, limit=False, planes=False):
         out["planes"], out["ped"] = dpl.cpu().numpy(), dped.cpu().numpy()
     plan.close()
     return out
+
+
+def fp64_reference(a, b, step, ia, mode, orc):
+    """Vectors of the reference's chain on numpy FP64 planes (any window
+    size): find_peaks(plane, 2, 1), fit_simple_gaussian, main.cpp:220-236."""
+    h, w = a.shape
+    grid = orc.grid_offsets(w, h, ia, ia, step, step)
+    planes, ped = reference_planes(a, b, grid, ia, mode)
+    vec = np.zeros((len(grid), 5))
+    peak = np.full(len(grid), -1, np.int64)
+    for i, (x, y) in enumerate(grid):
+        plane = planes[i] + ped[i]
+        xy, v = orc.find_peaks(plane, 2, 1)
+        if len(v) < 2:
+            continue
+        fx, fy = orc.fit_simple_gaussian(plane, int(xy[0, 0]), int(xy[0, 1]))
+        mx, my = x + ia // 2, y + ia // 2
+        vec[i] = (mx, h - my, mx - (x + fx), my - (y + fy), v[0] / v[1] if v[1] > 0 else 0.0)
+        peak[i] = xy[0, 1] * ia + xy[0, 0]
+    return {"vec": vec, "peak": peak, "grid": grid}
 
 
 def displacement_error(got, ref):
@@ -119,10 +152,10 @@ def test_fp64_pass_equals_certified_fp32_path():
 
 def test_precision_argument_errors():
     a = np.zeros((256, 256), np.uint16)
-    p16 = og.Plan(256, 256, np.uint16, 16, 8)
-    with pytest.raises(og.OpivError) as e:
-        p16.set_precision(og.PREC_TC_SPLIT_BF16)
-    assert e.value.status == og.ERR_UNSUPPORTED
+    # 16 px windows at x = 4 + 8 i: the generic kernel takes any x position
+    p16 = og.Plan(260, 256, np.uint16, 16, 8)
+    assert p16.grid()[0, 0] == 2
+    p16.set_precision(og.PREC_TC_SPLIT_BF16)
     pf = og.Plan(256, 256, np.float32, 32, 8)
     with pytest.raises(og.OpivError) as e:
         pf.set_precision(og.PREC_TC_BF16)
@@ -153,3 +186,62 @@ def test_precision_sweep_variants(variant):
         got = run(a, b, 8, precision)
         rms, mx, mm = displacement_error(got, ref)
         assert rms <= rms_t and mx <= max_t and mm <= mm_t, (variant, precision, rms, mx, mm)
+
+
+# ---- 16, 48 and 64 px windows: the generic tensor-core kernel ---------------------
+GENERIC = [(16, 8), (48, 24), (64, 32)]        # window, step on the 1024^2 u8 pair
+GENERIC_PLANE_RTOL = {og.PREC_TC_SPLIT_BF16: 5e-5, og.PREC_TC_BF16: 2e-2,
+                      og.PREC_TC_SPLIT_FP16: 1e-4, og.PREC_TC_FP16: 5e-3}
+
+
+@pytest.mark.parametrize("ia,step", GENERIC)
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_generic_planes_match_fp64_fft(ia, step, mode):
+    a, b = synth.config1()
+    for precision, rtol in GENERIC_PLANE_RTOL.items():
+        got = run(a, b, step, precision, mode=mode, planes=True, ia=ia)
+        ref, ped = reference_planes(a, b, got["grid"], ia, mode)
+        if precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT_FP16):
+            assert np.array_equal(got["ped"], ped)     # exact: integer sums below 2^24
+        err = np.abs(got["planes"] - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
+        assert err.max() <= rtol, f"{ia} px {precision}: plane error {err.max():.3e} of the plane peak"
+
+
+@pytest.mark.parametrize("ia,step", [(16, 4), (48, 12), (64, 16)])
+def test_generic_vectors_against_fp64(ia, step, orc):
+    """config-2 statistics on a 1024^2 crop at 75 % overlap: every tensor-
+    core precision inside its bounds against the FP64 reference (the FP64
+    pass for powers of 2, numpy FP64 planes through the reference's peak
+    search and fit for 48 px)."""
+    a, b = synth.config2(size=1024)
+    ref = fp64_reference(a, b, step, ia, og.CORR_COMPLEX, orc) if ia == 48 else run(a, b, step, og.PREC_FP64, ia=ia)
+    for precision, (rms_t, max_t, mm_t) in BOUNDS.items():
+        got = run(a, b, step, precision, ia=ia)
+        assert np.array_equal(got["grid"], ref["grid"])
+        rms, mx, mm = displacement_error(got, ref)
+        assert rms <= rms_t and mx <= max_t and mm <= mm_t, (ia, precision, rms, mx, mm)
+
+
+def test_generic_limited_search_and_errors():
+    a, b = synth.config1()
+    for ia, step in GENERIC:
+        ref = run(a, b, step, og.PREC_FP64, limit=True, ia=ia) if ia != 48 else None
+        got = run(a, b, step, og.PREC_TC_SPLIT_BF16, limit=True, ia=ia)
+        if ref is not None:
+            rms, mx, mm = displacement_error(got, ref)
+            assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH, (ia, rms, mx, mm)
+    # a 48 px plan takes no FFT precision and no adjoint; 40 px has no kernel
+    p48 = og.Plan(256, 256, np.uint16, 48, 8, tensor_core=og.PREC_TC_BF16)
+    for prec in (og.PREC_FP32, og.PREC_FP64):
+        with pytest.raises(og.OpivError) as e:
+            p48.set_precision(prec)
+        assert e.value.status == og.ERR_NOT_POW2
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 48, 8)
+    assert e.value.status == og.ERR_NOT_POW2
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 40, 8, tensor_core=og.PREC_TC_BF16)
+    assert e.value.status == og.ERR_UNSUPPORTED
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 48, 8, tensor_core=og.PREC_FP32)
+    assert e.value.status == og.ERR_ARG
