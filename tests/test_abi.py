@@ -84,6 +84,31 @@ def test_plan_validation_precedes_device(lib):
     assert e.value.status == og.ERR_ARG
 
 
+def test_tensor_core_plan_validation_precedes_device(lib):
+    """opiv_plan_create_tc: a tensor-core precision, then the grid checks,
+    then the window sizes that path takes (16, 32, 48, 64 px of u8/u16
+    frames; 48 px, which the FFT path rejects, included) -- all before any
+    device is touched."""
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 48, 12, tensor_core=og.PREC_FP32)
+    assert e.value.status == og.ERR_ARG
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 48, 12, tensor_core=9)
+    assert e.value.status == og.ERR_ARG
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 40, 8, tensor_core=og.PREC_TC_BF16)
+    assert e.value.status == og.ERR_UNSUPPORTED
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.float32, 48, 12, tensor_core=og.PREC_TC_BF16)
+    assert e.value.status == og.ERR_UNSUPPORTED
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(40, 256, np.uint16, 48, 12, tensor_core=og.PREC_TC_BF16)
+    assert e.value.status == og.ERR_IA_TOO_BIG
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(256, 256, np.uint16, 48, 12)
+    assert e.value.status == og.ERR_NOT_POW2
+
+
 def test_host_find_peaks_and_fit(lib, orc):
     rng = np.random.default_rng(1)
     for _ in range(20):
