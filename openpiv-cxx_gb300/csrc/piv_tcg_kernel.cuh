@@ -65,7 +65,8 @@ struct Geo {
     static constexpr int kParts = SPLIT ? 2 : 1;
     static constexpr int kOp = 512 * W;       // largest operand (hi part), bytes
     static constexpr int PS = W + 1;          // plane row stride (floats)
-    static constexpr int kXch = 4 * (R3 * 2 * W + WPT * 2 * W);
+    static constexpr int XS = 2 * W + 1;      // exchange row stride (floats), odd
+    static constexpr int kXch = 4 * (R3 + WPT) * XS;
     static constexpr int kPlane = 4 * R2 * PS;
     static constexpr int kScratch = ((kXch > kPlane ? kXch : kPlane) + 127) / 128 * 128;
     static constexpr int kTail = 256;
@@ -301,8 +302,8 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             const int r = tid;
             const bool ok = r < G::R2;
             const int wi = r / W, f = (r / H) & 1, kx = r % H;
-            float* xa = xch + (wi * H + kx) * 2 * W;            // frame a's row of this (window, k_x)
-            float* xp = xch + G::R3 * 2 * W + wi * 2 * W;       // frame b's slot-0 row of the window
+            float* xa = xch + (wi * H + kx) * G::XS;            // frame a's row of this (window, k_x)
+            float* xp = xch + (G::R3 + wi) * G::XS;             // frame b's slot-0 row of the window
             // frame a's rows, and frame b's slot-0 rows, into shared memory
 #pragma unroll 1
             for (int c0 = 0; c0 < 2 * W; c0 += 16) {
@@ -573,15 +574,28 @@ cudaError_t launch_t(const PivParams& p, int mode, int limit, const void* consts
     const uint64_t bit = 1ull << (dev & 63);
     if (!(attr_done.load() & bit)) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::kSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
-        int sms = 0, per_sm = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, G::kSmem);
-        if (e != cudaSuccess) return e;
-        // tensor memory: 512 columns per SM
-        const int tm = 512 / (int)G::kTmemCols;
-        per_sm = per_sm < tm ? per_sm : tm;
+        // resident CTAs per SM from each limit: shared memory (with the
+        // per-block reservation), registers, threads, tensor-memory columns
+        int sms = 0, smem_sm = 0, resv = 0, regs_sm = 0, thr_sm = 0;
+        cudaFuncAttributes fa{};
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev)) != cudaSuccess ||
+            (e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess)
+            return e;
+        int per_sm = smem_sm / (G::kSmem + (int)fa.sharedSizeBytes + resv);
+        const int regs = fa.numRegs > 0 ? (fa.numRegs + 7) / 8 * 8 : 1;
+        const int by_regs = regs_sm / (regs * kThreads), by_thr = thr_sm / kThreads;
+        const int by_tmem = 512 / (int)G::kTmemCols;
+        per_sm = per_sm < by_regs ? per_sm : by_regs;
+        per_sm = per_sm < by_thr ? per_sm : by_thr;
+        per_sm = per_sm < by_tmem ? per_sm : by_tmem;
         cap[dev & 63].store((per_sm > 0 ? per_sm : 1) * sms);
         attr_done.fetch_or(bit);
     }
