@@ -29,12 +29,14 @@
 //            the result is the swap_quadrants'ed plane minus its pedestal.
 //
 // One CTA of 4 warps runs tiles of 4 windows; warp w owns tensor-memory
-// lanes 32w .. 32w+31.  Every stage: CUDA cores write the operand into
-// shared memory (canonical no-swizzle layout, hi and lo parts), one thread
-// issues the MMAs and commits them to an mbarrier, all threads wait
-// (bounded) and read the accumulator back with tcgen05.ld.  Four CTAs
-// (54 KB of shared memory, 64 tensor-memory columns each) share an SM, so
-// the MMAs of some overlap the CUDA-core work of the others.
+// lanes 32w .. 32w+31.  Every stage: CUDA cores write the operand (hi and
+// lo parts) -- stage 1's pixels into tensor memory (tcgen05.st, each thread
+// its own lane's image row), the later operands into shared memory
+// (canonical no-swizzle layout) -- one thread issues the MMAs and commits
+// them to an mbarrier, all threads wait (bounded) and read the accumulator
+// back with tcgen05.ld.  Four CTAs (54 KB of shared memory, 128
+// tensor-memory columns each: 64 of accumulators, 64 of stage-1 operand)
+// share an SM, so the MMAs of some overlap the CUDA-core work of the others.
 #pragma once
 
 #include <atomic>
@@ -59,7 +61,8 @@ constexpr int kConstBytes = kTcNumMat * 2 * kMat;
 constexpr int kDataBytes = 34 * 1024;
 constexpr int kTailBytes = 768;                 // sums, origins, indices, row sums, mbarrier, TMEM slot, flag
 constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
-constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kA1 = 64;                    // TMEM column of the stage-1 operand (hi, then lo)
 constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
 constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (after the stage-3 operand)
 constexpr int kPRow = 36;                       // E4 plane row (floats), padded
@@ -154,6 +157,18 @@ __device__ __forceinline__ void mma3(uint32_t d, uint64_t a, uint64_t b, uint32_
     if (SPLIT) {
         tcx::mma_bf16(d, a, b + ((kTcNumMat * kMat) >> 4), idesc, true);
         tcx::mma_bf16(d, a + (kLo >> 4), b, idesc, true);
+    }
+}
+
+// The same with the A operand (hi part a_hi, lo part a_lo) in tensor memory.
+template <bool SPLIT>
+__device__ __forceinline__ void mma3_ta(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint64_t b, uint32_t idesc,
+                                        bool acc)
+{
+    tcx::mma_bf16_ta(d, a_hi, b, idesc, acc);
+    if (SPLIT) {
+        tcx::mma_bf16_ta(d, a_hi, b + ((kTcNumMat * kMat) >> 4), idesc, true);
+        tcx::mma_bf16_ta(d, a_lo, b, idesc, true);
     }
 }
 
@@ -252,7 +267,6 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     // parts), and the data buffer in the layouts of the four stages
     const uint64_t dB = tcx::sdesc(cst_a, 128, 512);
     auto mat = [&](int m, int ks) { return dB + (uint64_t)((m * kMat + ks * 256) >> 4); };
-    const uint64_t dA1 = tcx::sdesc(dat_a, 128, 512);     // K-major, 4 k-groups per row group
     const uint64_t dA2 = tcx::sdesc(dat_a, 2048, 128);    // MN-major, k-group stride 2 KB
     const uint64_t dA3 = tcx::sdesc(dat_a, 128, 1024);    // K-major, 8 k-groups per row group
     auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
@@ -321,50 +335,51 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         // number of window rows of this tile (VT: image rows below its top)
         const int vrows = VT ? (org[1].x >= 0 ? (org[2].x >= 0 ? (org[3].x >= 0 ? 3 : 2) : 1) : 0) * p.gdy + W
                              : 0;
-        if constexpr (VT) {
-            // ---- stage-1 operand: rows R = f * 64 + y of the tile's image
-            // rows (y < vrows <= 56), K-major 128 x 32 (hi | lo)
-            const int2 o = org[0];
-            typename Raw<PixT>::type raw[4];
+        // ---- stage-1 operand in tensor memory: thread tid owns lane tid.
+        // VT: row R = tid = f * 64 + y of the tile's image rows (y < vrows);
+        // otherwise rows R = m1 * 128 + tid = (2 m1 + wl) * 64 + f * 32 + y.
+        // A row's 32 pixels, widened (frame B rows times (-1)^y: its column
+        // spectrum comes out rotated by 16 in k_y, see E2), fill 16 columns
+        // of the hi part (and 16 of the lo part): pixel 2c in the low half
+        // of column c.
+        {
+            constexpr int NM = VT ? 1 : 2;
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                const int f = t >> 1, y = R & 63;
-                raw[t] = (o.x >= 0 && y < vrows)
-                             ? load_raw<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g)
-                             : Raw<PixT>::zero();
-            }
-            const float sb = (it_r7 & 1) ? -1.f : 1.f;   // frame B rows times (-1)^y
+            for (int m1 = 0; m1 < NM; ++m1) {
+                const int R = m1 * 128 + tid;
+                int f, y;
+                const PixT* row = nullptr;
+                if constexpr (VT) {
+                    f = R >> 6;
+                    y = R & 63;
+                    const int2 o = org[0];
+                    if (o.x >= 0 && y < vrows) row = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x;
+                } else {
+                    f = (R >> 5) & 1;
+                    y = R & 31;
+                    const int2 o = org[R >> 6];
+                    if (o.x >= 0) row = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x;
+                }
+                typename Raw<PixT>::type raw[4];
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                float px[8];
-                widen8<PixT>(raw[t], px, ((t >> 1) ? sb : 1.f) * kPix);
-                put8<F16, SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
-            }
-        } else {
-        // ---- stage-1 operand: window rows, K-major 256 x 32 (hi | lo);
-        // rows R = (2 m1 + wl) * 64 + f * 32 + y.  All eight loads are in
-        // flight before the first conversion.
-            typename Raw<PixT>::type raw[8];
+                for (int g = 0; g < 4; ++g) raw[g] = row ? load_raw<PixT>(row + 8 * g) : Raw<PixT>::zero();
+                const float sg = ((f && (y & 1)) ? -1.f : 1.f) * kPix;
+                uint32_t hw[16], lw[16];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
-                const int2 o = org[w];
-                raw[t] = (o.x >= 0)
-                             ? load_raw<PixT>((f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g)
-                             : Raw<PixT>::zero();
-            }
-            // frame B rows times (-1)^y: its column spectrum comes out rotated
-            // by 16 in k_y (see E2); rows R have f = t & 1, y & 1 = R & 1
-            const float sb = (it_r7 & 1) ? -1.f : 1.f;
+                for (int g = 0; g < 4; ++g) {
+                    float px[8];
+                    widen8<PixT>(raw[g], px, sg);
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int R = (it_rg + 4 * t) * 8 + it_r7;
-                float px[8];
-                widen8<PixT>(raw[t], px, ((t & 1) ? sb : 1.f) * kPix);
-                put8<F16, SPLIT>(dat, ((R >> 3) * 4 + it_g) * 128 + it_r7 * 16, px);
+                    for (int j = 0; j < 4; ++j) {
+                        hw[4 * g + j] = pack2<F16>(px[2 * j], px[2 * j + 1]);
+                        if (SPLIT) {
+                            const float2 hf = unpack2<F16>(hw[4 * g + j]);
+                            lw[4 * g + j] = pack2<F16>(px[2 * j] - hf.x, px[2 * j + 1] - hf.y);
+                        }
+                    }
+                }
+                tcx::tmem_st16(tlane + kA1 + 16 * m1, hw);
+                if (SPLIT) tcx::tmem_st16(tlane + kA1 + 16 * NM + 16 * m1, lw);
             }
         }
         tcx::fence_proxy();
@@ -372,15 +387,17 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         __syncthreads();
         if (*abort_flag) break;
 
-        // ---- stage 1: H = X * G, one (VT) or two M-tiles of 128 rows
+        // ---- stage 1: H = X * G, one (VT) or two M-tiles of 128 rows, the
+        // operand X in tensor memory
         if (tid == 0) {
             tcx::fence_after();
+            constexpr int NM = VT ? 1 : 2;
 #pragma unroll
-            for (int m1 = 0; m1 < (VT ? 1 : 2); ++m1)
+            for (int m1 = 0; m1 < NM; ++m1)
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
-                    mma3<SPLIT>(tbase + 32 * m1, dA1 + off(m1 * 8192 + ks * 256), mat(kTcG1, ks),
-                                kIdK32, ks > 0);
+                    mma3_ta<SPLIT>(tbase + 32 * m1, tbase + kA1 + 16 * m1 + 8 * ks,
+                                   tbase + kA1 + 16 * NM + 16 * m1 + 8 * ks, mat(kTcG1, ks), kIdK32, ks > 0);
             tcx::commit(mbar);
         }
         // the next tile's window rows into L2 while this tile computes

@@ -46,6 +46,30 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
                  :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(accumulate ? 1 : 0));
 }
 
+// The same with the A operand in tensor memory: a_tmem addresses lane 0 of
+// M rows (row m in lane m), K = 16 elements in 8 consecutive 32-bit
+// columns, element 2c in the low and 2c + 1 in the high half of column c.
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            bool accumulate)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+                 :: "r"(d_tmem), "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate ? 1 : 0));
+}
+
+// 16 consecutive 32-bit columns of this warp's 32 lanes from registers
+// (thread t writes lane taddr.lane + t); waits for the store.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* w)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+                 "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n"
+                 "tcgen05.wait::st.sync.aligned;"
+                 :: "r"(taddr), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]),
+                    "r"(w[7]), "r"(w[8]), "r"(w[9]), "r"(w[10]), "r"(w[11]), "r"(w[12]), "r"(w[13]), "r"(w[14]),
+                    "r"(w[15])
+                 : "memory");
+}
+
 __device__ __forceinline__ void commit(uint64_t* mbar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
