@@ -491,14 +491,36 @@ def run_batch(args):
 
     sampler = ClockSampler(dev)
     sampler.start()
+    # streams schedule: every pair's pass chain on 8 fork streams
     for _ in range(args.warmup):
         batch.run(use_graph=False, stream=h)
     eager = timed(False, args.steps)
     for _ in range(args.warmup):
         batch.run(use_graph=True, stream=h)
     launches_before = og.kernel_launch_count()
-    graph = timed(True, args.steps)
-    gpu_launches = og.kernel_launch_count() - launches_before
+    graph_streams = timed(True, args.steps)
+    launches_streams = og.kernel_launch_count() - launches_before
+    # queue schedule: per pass one persistent kernel over a device work queue
+    # of all pairs' windows; untuned (resident grid, chunk 1), then autotuned
+    batch.set_schedule(og.BATCH_QUEUE)
+    for _ in range(args.warmup):
+        batch.run(use_graph=True, stream=h)
+    graph_queue0 = timed(True, args.steps)
+    t_tune = time.perf_counter()
+    batch.autotune(stream=h)
+    t_tune = time.perf_counter() - t_tune
+    tuning = [batch.tuning(k) for k in range(n_pass)]
+    for _ in range(args.warmup):
+        batch.run(use_graph=True, stream=h)
+    launches_before = og.kernel_launch_count()
+    graph_queue = timed(True, args.steps)
+    launches_queue = og.kernel_launch_count() - launches_before
+    # windows the exact FP64 pass re-decided, per pass (peak codes' flag bit)
+    exact_per_pass = [int(sum(np.count_nonzero(batch.results(i, k)[1] & og.PEAK_EXACT)
+                              for i in range(len(sizes)))) for k in range(n_pass)]
+    use_queue = graph_queue <= graph_streams
+    graph = graph_queue if use_queue else graph_streams
+    gpu_launches = launches_queue if use_queue else launches_streams
 
     # end to end: pinned host frames in, every pair's final-pass vectors out
     pinned = [(torch.from_numpy(a).pin_memory(), torch.from_numpy(b).pin_memory())
@@ -518,13 +540,23 @@ def run_batch(args):
         # its vectors come back once its last pass ends
         batch.process_into(*ptrs)
 
-    e2e_step()
-    dist_barrier(world)
     e2e_steps = max(1, args.steps // 4)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_time(schedule):
+        batch.set_schedule(schedule)
+        if schedule == og.BATCH_QUEUE:
+            batch.run(use_graph=True, stream=h)   # records the queue graph the call replays
+            stream.synchronize()
         e2e_step()
-    t_e2e = dist_max(time.perf_counter() - t0, world)
+        dist_barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        return dist_max(time.perf_counter() - t0, world)
+
+    t_e2e_streams = e2e_time(og.BATCH_STREAMS)
+    t_e2e_queue = e2e_time(og.BATCH_QUEUE)
+    t_e2e = min(t_e2e_streams, t_e2e_queue)
     clocks = sampler.stop()
     batch.close()
     if rank != 0:
@@ -543,16 +575,37 @@ def run_batch(args):
                    "sizes": {f"{w}x{h}": sizes.count((w, h)) for w, h in sorted(set(sizes))},
                    "passes": BATCH_PASSES, "final_vectors_per_step": final,
                    "windows_per_step_all_passes": total, "mode": "complex",
-                   "submission": "CUDA graph of all pairs' passes on 8 forked streams",
+                   "submission": ("CUDA graph of the queue schedule: per pass one persistent FP32 "
+                                  "kernel over a device work queue of all pairs' windows + one exact "
+                                  "launch, autotuned grid and chunk" if use_queue else
+                                  "CUDA graph of all pairs' passes on 8 forked streams"),
                    "l2": f"{sum(2 * w * h * 2 for w, h in sizes) / 1e9:.2f} GB of frames per "
                          f"step (> 129 MB L2)",
                    "parallelism": f"replicas x{world}"},
         "windows_per_s_all_passes": args.steps * total * world / graph,
         "eager_value": args.steps * final * world / eager,
+        "schedules": {
+            "streams_graph": args.steps * final * world / graph_streams,
+            "streams_eager": args.steps * final * world / eager,
+            "queue_graph_untuned": args.steps * final * world / graph_queue0,
+            "queue_graph_autotuned": args.steps * final * world / graph_queue,
+            "launches_per_step": {"streams": launches_streams / args.steps,
+                                  "queue": launches_queue / args.steps},
+            "exact_windows_per_pass": exact_per_pass,
+            "autotune": {"seconds": t_tune,
+                         "per_pass": [{"ia": BATCH_PASSES[k][0], "ctas_per_sm": c, "chunk": ch,
+                                       "resident_limit": mx, "pass_ms": ms}
+                                      for k, (c, ch, mx, ms) in enumerate(tuning)]},
+        },
         "e2e": {"value": e2e_steps * final * world / t_e2e, "unit": "vectors/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "call": "opiv_batch_process (pinned host frames; per-pair uploads, pass chains "
-                        "and downloads overlapped)"},
+                "call": ("opiv_batch_process, streams schedule (pinned host frames; per-pair "
+                         "uploads, pass chains and downloads overlapped)"
+                         if t_e2e_streams <= t_e2e_queue else
+                         "opiv_batch_process, queue schedule (all uploads, the queue graph, "
+                         "all downloads)"),
+                "streams": e2e_steps * final * world / t_e2e_streams,
+                "queue": e2e_steps * final * world / t_e2e_queue},
         "gpu_launches": gpu_launches,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,

@@ -275,6 +275,47 @@ int opiv_batch_process(opiv_batch* batch, const void* const* frames_a, const voi
                        const size_t* pitch_bytes, opiv_vector* const* out_vec,
                        int32_t* const* out_peak);
 
+/* Schedules of a batch (no counterpart in the reference).
+ * OPIV_BATCH_STREAMS (the default): every pair's pass chain on a fork
+ *   stream, two launches per pair and pass.
+ * OPIV_BATCH_QUEUE: per pass and group of up to 64 pairs, one persistent
+ *   kernel over a device work queue that holds the group's windows (CTAs
+ *   take tasks from an atomic counter; no kernel waits on another), then one
+ *   exact re-decision launch over the group's flagged windows: two launches
+ *   per pass for batches of up to 64 pairs.  Results are identical to the
+ *   streams schedule.  Window sizes 16, 32 and 64 (the FP32 kernels);
+ *   OPIV_ERR_UNSUPPORTED otherwise, and when a group's combined window
+ *   count exceeds 2^31 - 1.  opiv_batch_process under this schedule uploads
+ *   every pair, runs the passes, then downloads (no copy / pass overlap).
+ * Changing the schedule or the tuning drops a recorded graph; the next
+ * opiv_batch_run with use_graph = 1 records a new one. */
+enum { OPIV_BATCH_STREAMS = 0, OPIV_BATCH_QUEUE = 1 };
+int opiv_batch_set_schedule(opiv_batch* batch, int schedule);
+/* Queue tuning of pass `pass`: the persistent grid has ctas_per_sm CTAs per
+ * SM (1 .. 32; above the kernel's resident limit the extra CTAs simply run
+ * later) and each warp of a CTA takes `chunk` tasks (1 .. 1024) per dequeue
+ * (16, 32 px: a CTA takes 4 * chunk consecutive tasks, its warps
+ * interleaved; 64 px: a CTA runs one task at a time).  ctas_per_sm = 0
+ * launches the same work list with one CTA per task group instead (the
+ * hardware's block scheduler hands them out; no persistent loop, chunk
+ * unused).  Untuned passes use the persistent grid at the resident limit
+ * and chunk 1. */
+int opiv_batch_set_tuning(opiv_batch* batch, int pass, int ctas_per_sm, int chunk);
+/* Current tuning of pass `pass`; *max_ctas_per_sm (may be null) receives the
+ * queue kernel's resident CTAs per SM (0 before the queue's first use) and
+ * *tuned_ms (may be null) the autotuner's fastest time of the pass in ms (0
+ * when the pass's tuning did not come from the autotuner). */
+int opiv_batch_get_tuning(const opiv_batch* batch, int pass, int* ctas_per_sm, int* chunk,
+                          int* max_ctas_per_sm, float* tuned_ms);
+/* Autotuner: selects the queue schedule and, pass after pass, times every
+ * candidate (the hardware-dispatched list; persistent grids of 1 .. resident
+ * limit (at most 4) CTAs per SM with chunk 1, 2, 4, 8; fastest of
+ * two timed runs after one warm-up, CUDA events on `stream`) on the frames
+ * the batch holds now, and keeps the fastest per pass.  The pass chain runs
+ * in order, so each pass is tuned on the real offsets of the one before;
+ * the batch's results afterwards are those of a normal run.  Synchronous. */
+int opiv_batch_autotune(opiv_batch* batch, void* stream);
+
 /* ---- allocation-free pass ------------------------------------------------ */
 /* No counterpart in the reference.  The same pass as opiv_process_pair_device
  * for callers that must not allocate device memory once they are running

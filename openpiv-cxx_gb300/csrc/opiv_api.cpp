@@ -256,15 +256,12 @@ PivParams base_params(const opiv_plan* p)
 // pass of a multi-pass chain, whose integer displacements offset frame B.
 // flag_count / flag_list: the exact pass's scratch (null: the plan's own;
 // passes that may run concurrently need their own).
-int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_vector* vec,
-             int32_t* peak, cudaStream_t s, const opiv_plan* prev = nullptr,
-             unsigned int* flag_count = nullptr, int32_t* flag_list = nullptr)
+// The parameters of one pass of plan p over frames fa, fb; `prev`: the
+// previous pass of a multi-pass chain (window offsetting) or null.
+PivParams pass_params(const opiv_plan* p, const void* fa, const void* fb, size_t pitch,
+                      opiv_vector* vec, int32_t* peak, const opiv_plan* prev)
 {
     PivParams k = base_params(p);
-    if (flag_count) {
-        k.flag_count = flag_count;
-        k.flag_list = flag_list;
-    }
     k.fa = fa;
     k.fb = fb;
     k.pitch = pitch;
@@ -280,6 +277,18 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.pgnx = (int)prev->g.xc;
         k.pgny = (int)prev->g.yc;
         k.pw = (int)prev->ia;
+    }
+    return k;
+}
+
+int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_vector* vec,
+             int32_t* peak, cudaStream_t s, const opiv_plan* prev = nullptr,
+             unsigned int* flag_count = nullptr, int32_t* flag_list = nullptr)
+{
+    PivParams k = pass_params(p, fa, fb, pitch, vec, peak, prev);
+    if (flag_count) {
+        k.flag_count = flag_count;
+        k.flag_list = flag_list;
     }
     CUDA_TRY(cudaMemsetAsync(k.flag_count, 0, sizeof(unsigned int), s));
     if (is_tc(p->precision)) {
@@ -803,6 +812,23 @@ int opiv_multipass_results(opiv_multipass* mp, int pass, opiv_vector* out_vec, i
 }
 
 // ---- batches of image pairs ----------------------------------------------------
+// Device work queues of one pass of a batch (OPIV_BATCH_QUEUE): the pairs
+// in groups of up to kQueueMaxItems, one queue (two launches) per group.
+struct batch_queue_pass {
+    std::vector<PivQueue> groups;       // host copies, passed by value at launch
+    unsigned int* d_ctr = nullptr;      // per group: dequeue head, flagged windows
+    int32_t* d_flags = nullptr;         // per group: its flag list (combined window numbers)
+    PivParams* d_items = nullptr;       // per group: its descriptors (kQueueMaxItems slots)
+    uint8_t* d_task_item = nullptr;     // per group: the pair of every task
+    int ia = 0, dtype = 0, mode = 0, limit = 0;
+    bool vec = true;                    // every pair's A rows 16-byte aligned
+    int max_ctas = 0;                   // resident CTAs per SM of the queue kernel
+    int exact_blocks = kExactBlocks;    // CTAs of the exact launch: every resident slot
+    int ctas_per_sm = -1;               // tuning: -1 untuned (the resident limit), 0 hardware dispatch
+    int chunk = 1;                      // tuning: tasks per dequeue
+    float tuned_ms = 0.f;               // the autotuner's fastest pass time
+};
+
 struct opiv_batch {
     std::vector<opiv_multipass*> pairs;
     std::vector<void*> d_fa, d_fb;
@@ -816,7 +842,170 @@ struct opiv_batch {
     // opiv_batch_process: copy streams and one upload / done event per pair
     cudaStream_t up = nullptr, down = nullptr;
     std::vector<cudaEvent_t> ev_up, ev_done;
+    // OPIV_BATCH_QUEUE: one work queue per pass, built on first use; the
+    // tuning of a pass may be set before that (kept in tune_*)
+    int schedule = OPIV_BATCH_STREAMS;
+    std::vector<batch_queue_pass> qp;
+    std::vector<int> tune_ctas, tune_chunk;
+    int sms = 0;
 };
+
+namespace {
+
+void batch_drop_graph(opiv_batch* b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+void batch_free_queue(opiv_batch* b)
+{
+    for (batch_queue_pass& q : b->qp) {
+        cudaFree(q.d_ctr);
+        cudaFree(q.d_flags);
+        cudaFree(q.d_items);
+        cudaFree(q.d_task_item);
+    }
+    b->qp.clear();
+}
+
+// Builds every pass's work queues (descriptors of all pairs, counters and
+// flag lists on the device); the batch's device is current.
+int batch_queue_setup(opiv_batch* b)
+{
+    if (!b->qp.empty()) return OPIV_OK;
+    const int n = (int)b->pairs.size();
+    const int n_pass = (int)b->pairs[0]->passes.size();
+    const int n_groups = (n + kQueueMaxItems - 1) / kQueueMaxItems;
+    if (b->sms == 0) CUDA_TRY(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
+    std::vector<batch_queue_pass> qs(n_pass);
+    int rc = OPIV_OK;
+    for (int k = 0; k < n_pass && rc == OPIV_OK; ++k) {
+        batch_queue_pass& q = qs[k];
+        const opiv_plan* p0 = b->pairs[0]->passes[k];
+        q.ia = (int)p0->ia;
+        q.dtype = p0->dtype;
+        q.mode = kernel_mode(p0->mode);
+        q.limit = p0->limit;
+        if (!fp32_supports(q.ia) || p0->precision != OPIV_PREC_FP32) {
+            rc = fail(OPIV_ERR_UNSUPPORTED, "the queue schedule runs 16, 32 and 64 px FP32 passes only");
+            break;
+        }
+        q.groups.resize(n_groups);
+        std::vector<int64_t> flag_off(n_groups + 1, 0);   // each group's flag list in d_flags
+        std::vector<int64_t> task_off(n_groups + 1, 0);   // each group's task pairs in d_task_item
+        std::vector<uint8_t> task_item;
+        const size_t px = px_bytes(q.dtype);
+        for (int g = 0; g < n_groups && rc == OPIV_OK; ++g) {
+            PivQueue& pq = q.groups[g];
+            const int i0 = g * kQueueMaxItems, i1 = std::min(n, i0 + kQueueMaxItems);
+            pq.n_items = i1 - i0;
+            int64_t tasks = 0, wins = 0;
+            for (int i = i0; i < i1; ++i) {
+                const opiv_plan* p = b->pairs[i]->passes[k];
+                const opiv_plan* prev = k ? b->pairs[i]->passes[k - 1] : nullptr;
+                PivParams it = pass_params(p, b->d_fa[i], b->d_fb[i], b->pitch[i], p->d_vec, p->d_peak, prev);
+                pq.first_task[i - i0] = (int)tasks;
+                pq.first_win[i - i0] = (int)wins;
+                it.flag_base = (int32_t)wins;
+                const int nt = fp32_queue_tasks(q.ia, p->n_win);
+                task_item.insert(task_item.end(), (size_t)nt, (uint8_t)(i - i0));
+                tasks += nt;
+                wins += p->n_win;
+                if (tasks > INT32_MAX || wins > INT32_MAX) {
+                    rc = fail(OPIV_ERR_UNSUPPORTED, "a queue of %d pairs holds more than 2^31 - 1 windows",
+                              kQueueMaxItems);
+                    break;
+                }
+                // the condition of the single-pair kernel's 128-bit row loads
+                q.vec = q.vec && ((uintptr_t)it.fa % 16 == 0) && ((uintptr_t)it.fb % 16 == 0) &&
+                        (it.pitch % 16 == 0) && (((size_t)it.gx0 * px) % 16 == 0) &&
+                        (((size_t)it.gdx * px) % 16 == 0) && (((size_t)q.ia * px) % 16 == 0);
+                pq.items[i - i0] = it;
+            }
+            pq.first_task[pq.n_items] = (int)tasks;
+            pq.first_win[pq.n_items] = (int)wins;
+            flag_off[g + 1] = flag_off[g] + (wins > 0 ? wins : 1);
+            task_off[g + 1] = task_off[g] + tasks;
+        }
+        if (rc != OPIV_OK) break;
+        cudaError_t e;
+        if ((e = cudaMalloc(&q.d_ctr, 2 * sizeof(unsigned int) * n_groups)) != cudaSuccess ||
+            (e = cudaMalloc(&q.d_flags, sizeof(int32_t) * flag_off[n_groups])) != cudaSuccess ||
+            (e = cudaMalloc(&q.d_items, sizeof(PivParams) * kQueueMaxItems * n_groups)) != cudaSuccess ||
+            (e = cudaMalloc(&q.d_task_item, task_item.size() + 1)) != cudaSuccess) {
+            rc = cuda_fail(e, "cudaMalloc(work queue)");
+            break;
+        }
+        for (int g = 0; g < n_groups && rc == OPIV_OK; ++g) {
+            PivQueue& pq = q.groups[g];
+            pq.head = q.d_ctr + 2 * g;
+            pq.flag_count = q.d_ctr + 2 * g + 1;
+            pq.flag_list = q.d_flags + flag_off[g];
+            for (int j = 0; j < pq.n_items; ++j) {   // the group's one flag list
+                pq.items[j].flag_count = q.d_ctr + 2 * g + 1;
+                pq.items[j].flag_list = q.d_flags + flag_off[g];
+            }
+            pq.items_g = q.d_items + (size_t)kQueueMaxItems * g;
+            pq.task_item = q.d_task_item + task_off[g];
+            if ((e = cudaMemcpy(q.d_items + (size_t)kQueueMaxItems * g, pq.items, sizeof(PivParams) * pq.n_items,
+                                cudaMemcpyHostToDevice)) != cudaSuccess)
+                rc = cuda_fail(e, "cudaMemcpy(work queue)");
+        }
+        if (rc != OPIV_OK) break;
+        if (!task_item.empty() &&
+            (e = cudaMemcpy(q.d_task_item, task_item.data(), task_item.size(), cudaMemcpyHostToDevice)) !=
+                cudaSuccess) {
+            rc = cuda_fail(e, "cudaMemcpy(work queue)");
+            break;
+        }
+        const cudaError_t oe =
+            queue_piv_fp32(q.groups[0], q.ia, q.dtype, q.mode, q.limit, q.vec, 0, &q.max_ctas, nullptr);
+        if (oe != cudaSuccess) {
+            rc = cuda_fail(oe, "queue kernel occupancy");
+            break;
+        }
+        if (q.max_ctas < 1) q.max_ctas = 1;
+        // flagged windows are few but each costs ~0.1 ms of FP64 latency in one
+        // CTA; as many run at once as fit, so the pass waits about one round
+        q.exact_blocks = exact_queue_max_ctas_per_sm(q.ia) * b->sms;
+        q.ctas_per_sm = b->tune_ctas[k];
+        q.chunk = b->tune_chunk[k];
+    }
+    b->qp.swap(qs);
+    if (rc != OPIV_OK) batch_free_queue(b);   // a failed set-up's partial buffers
+    return rc;
+}
+
+// Pass k of the queue schedule on stream s: counters reset, then per group
+// of pairs the persistent FP32 kernel and the exact re-decision of the
+// group's flagged windows.
+int batch_queue_pass_enqueue(opiv_batch* b, int k, cudaStream_t s)
+{
+    batch_queue_pass& q = b->qp[k];
+    // CTAs of the persistent grid; 0: the hardware-dispatched list kernel
+    const int ctas = q.ctas_per_sm >= 0 ? q.ctas_per_sm : q.max_ctas;
+    CUDA_TRY(cudaMemsetAsync(q.d_ctr, 0, 2 * sizeof(unsigned int) * q.groups.size(), s));
+    for (PivQueue& pq : q.groups) {
+        pq.chunk = q.chunk;
+        CUDA_TRY(queue_piv_fp32(pq, q.ia, q.dtype, q.mode, q.limit, q.vec, ctas * b->sms, nullptr, s));
+        ++g_launches;
+        CUDA_TRY(launch_piv_exact_queue(pq, q.ia, q.dtype, q.mode, q.limit, q.exact_blocks, s));
+        ++g_launches;
+    }
+    return OPIV_OK;
+}
+
+int batch_queue_enqueue(opiv_batch* b, cudaStream_t s)
+{
+    int rc = batch_queue_setup(b);
+    for (int k = 0; k < (int)b->qp.size() && rc == OPIV_OK; ++k) rc = batch_queue_pass_enqueue(b, k, s);
+    return rc;
+}
+
+}  // namespace
 
 int opiv_batch_destroy(opiv_batch* b)
 {
@@ -824,9 +1013,9 @@ int opiv_batch_destroy(opiv_batch* b)
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(b->device);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
     if (b->main) cudaStreamSynchronize(b->main);
+    batch_drop_graph(b);
+    batch_free_queue(b);
     for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
     if (b->main) cudaStreamDestroy(b->main);
     if (b->up) cudaStreamDestroy(b->up);
@@ -861,6 +1050,8 @@ int opiv_batch_create(opiv_batch** out, int n_pairs, const uint32_t* widths, con
         }
         b->pairs.push_back(mp);
     }
+    b->tune_ctas.assign(n_passes, -1);
+    b->tune_chunk.assign(n_passes, 1);
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(device);
@@ -956,18 +1147,20 @@ int opiv_batch_run(opiv_batch* b, int use_graph, void* stream)
     cudaSetDevice(b->device);
     auto done = [&](int st) { cudaSetDevice(prev); return st; };
     cudaStream_t s = stream ? (cudaStream_t)stream : b->main;
-    if (!use_graph) return done(batch_enqueue(b, s));
+    const bool queue = b->schedule == OPIV_BATCH_QUEUE;
+    auto enqueue = [&](cudaStream_t st) { return queue ? batch_queue_enqueue(b, st) : batch_enqueue(b, st); };
+    if (!use_graph) return done(enqueue(s));
     cudaError_t e;
     if (!b->exec) {
         // one eager run first: one-time kernel attribute set-up happens
         // outside the capture
-        int rc = batch_enqueue(b, s);
+        int rc = enqueue(s);
         if (rc != OPIV_OK) return done(rc);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return done(cuda_fail(e, "cudaStreamSynchronize"));
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
             return done(cuda_fail(e, "cudaStreamBeginCapture"));
         const int64_t counted = g_launches;   // a capture launches nothing
-        rc = batch_enqueue(b, s);
+        rc = enqueue(s);
         g_launches = counted;
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(s, &g);
@@ -982,8 +1175,131 @@ int opiv_batch_run(opiv_batch* b, int use_graph, void* stream)
         return done(OPIV_OK);   // the eager run has produced this call's results
     }
     if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return done(cuda_fail(e, "cudaGraphLaunch"));
-    g_launches += 2 * (int64_t)b->pairs.size() * (int64_t)b->pairs[0]->passes.size();
+    const int64_t per_pass = queue ? (int64_t)(b->pairs.size() + kQueueMaxItems - 1) / kQueueMaxItems
+                                   : (int64_t)b->pairs.size();
+    g_launches += 2 * per_pass * (int64_t)b->pairs[0]->passes.size();
     return done(OPIV_OK);
+}
+
+int opiv_batch_set_schedule(opiv_batch* b, int schedule)
+{
+    if (!b) return fail(OPIV_ERR_ARG, "batch is null");
+    if (schedule != OPIV_BATCH_STREAMS && schedule != OPIV_BATCH_QUEUE)
+        return fail(OPIV_ERR_ARG, "unknown batch schedule %d", schedule);
+    if (schedule == b->schedule) return OPIV_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->main);
+    batch_drop_graph(b);
+    cudaSetDevice(prev);
+    b->schedule = schedule;
+    return OPIV_OK;
+}
+
+int opiv_batch_set_tuning(opiv_batch* b, int pass, int ctas_per_sm, int chunk)
+{
+    if (!b) return fail(OPIV_ERR_ARG, "batch is null");
+    if (pass < 0 || pass >= (int)b->tune_ctas.size()) return fail(OPIV_ERR_ARG, "no such pass");
+    if (ctas_per_sm < 0 || ctas_per_sm > 32) return fail(OPIV_ERR_ARG, "ctas_per_sm %d outside 0 .. 32", ctas_per_sm);
+    if (chunk < 1 || chunk > 1024) return fail(OPIV_ERR_ARG, "chunk %d outside 1 .. 1024", chunk);
+    b->tune_ctas[pass] = ctas_per_sm;
+    b->tune_chunk[pass] = chunk;
+    if (!b->qp.empty()) {
+        b->qp[pass].ctas_per_sm = ctas_per_sm;
+        b->qp[pass].chunk = chunk;
+        b->qp[pass].tuned_ms = 0.f;
+    }
+    if (b->exec) {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(b->device);
+        cudaStreamSynchronize(b->main);
+        batch_drop_graph(b);
+        cudaSetDevice(prev);
+    }
+    return OPIV_OK;
+}
+
+int opiv_batch_get_tuning(const opiv_batch* b, int pass, int* ctas_per_sm, int* chunk, int* max_ctas_per_sm,
+                          float* tuned_ms)
+{
+    if (!b || !ctas_per_sm || !chunk) return fail(OPIV_ERR_ARG, "null argument");
+    if (pass < 0 || pass >= (int)b->tune_ctas.size()) return fail(OPIV_ERR_ARG, "no such pass");
+    const int mx = b->qp.empty() ? 0 : b->qp[pass].max_ctas;
+    *ctas_per_sm = b->tune_ctas[pass] >= 0 ? b->tune_ctas[pass] : mx;
+    *chunk = b->tune_chunk[pass];
+    if (max_ctas_per_sm) *max_ctas_per_sm = mx;
+    if (tuned_ms) *tuned_ms = b->qp.empty() ? 0.f : b->qp[pass].tuned_ms;
+    return OPIV_OK;
+}
+
+int opiv_batch_autotune(opiv_batch* b, void* stream)
+{
+    if (!b) return fail(OPIV_ERR_ARG, "batch is null");
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->main;
+    CUDA_TRY_D(cudaStreamSynchronize(s));
+    batch_drop_graph(b);
+    b->schedule = OPIV_BATCH_QUEUE;
+    int rc = batch_queue_setup(b);
+    if (rc != OPIV_OK) return done(rc);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY_D(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return done(fail(OPIV_ERR_CUDA, "cudaEventCreate"));
+    }
+    static const int kChunks[] = { 1, 2, 4, 8 };
+    for (int k = 0; k < (int)b->qp.size() && rc == OPIV_OK; ++k) {
+        batch_queue_pass& q = b->qp[k];
+        float best = 3.4e38f;
+        int best_c = q.max_ctas, best_k = 1;
+        const int max_c = q.max_ctas < 4 ? q.max_ctas : 4;
+        for (int c = 0; c <= max_c && rc == OPIV_OK; ++c)
+            for (int ch : kChunks) {
+                if (c == 0 && ch != 1) continue;   // the list kernel has no chunk
+                q.ctas_per_sm = c;
+                q.chunk = ch;
+                float t_min = 3.4e38f;
+                for (int r = 0; r < 3 && rc == OPIV_OK; ++r) {   // one warm-up, two timed
+                    cudaEventRecord(e0, s);
+                    rc = batch_queue_pass_enqueue(b, k, s);
+                    cudaEventRecord(e1, s);
+                    if (rc != OPIV_OK) break;
+                    cudaError_t e = cudaEventSynchronize(e1);
+                    if (e != cudaSuccess) {
+                        rc = cuda_fail(e, "autotune run");
+                        break;
+                    }
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (r > 0 && ms < t_min) t_min = ms;
+                }
+                if (rc != OPIV_OK) break;
+                if (t_min < best) {
+                    best = t_min;
+                    best_c = c;
+                    best_k = ch;
+                }
+            }
+        if (rc != OPIV_OK) break;
+        q.ctas_per_sm = best_c;
+        q.chunk = best_k;
+        q.tuned_ms = best;
+        b->tune_ctas[k] = best_c;
+        b->tune_chunk[k] = best_k;
+        // the pass once more with its choice: the next pass reads its offsets
+        rc = batch_queue_pass_enqueue(b, k, s);
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == OPIV_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+    return done(rc);
 }
 
 int opiv_batch_process(opiv_batch* b, const void* const* frames_a, const void* const* frames_b,
@@ -1016,6 +1332,40 @@ int opiv_batch_process(opiv_batch* b, const void* const* frames_a, const void* c
                 return done(cuda_fail(e, "cudaEventCreateWithFlags"));
             b->ev_done.push_back(ed);
         }
+    }
+    if (b->schedule == OPIV_BATCH_QUEUE) {
+        // every pair up, the queue passes (a recorded graph if there is
+        // one), every pair's final vectors down; all on the batch's stream
+        cudaStream_t s = b->main;
+        for (int i = 0; i < n; ++i) {
+            const opiv_plan* p0 = b->pairs[i]->passes[0];
+            const size_t row = (size_t)p0->img_w * px_bytes(p0->dtype);
+            CUDA_TRY_D(cudaMemcpy2DAsync(b->d_fa[i], b->pitch[i], frames_a[i], pitch_bytes[i], row,
+                                         p0->img_h, cudaMemcpyHostToDevice, s));
+            CUDA_TRY_D(cudaMemcpy2DAsync(b->d_fb[i], b->pitch[i], frames_b[i], pitch_bytes[i], row,
+                                         p0->img_h, cudaMemcpyHostToDevice, s));
+        }
+        if (b->exec) {
+            CUDA_TRY_D(cudaGraphLaunch(b->exec, s));
+            g_launches += 2 * (int64_t)((n + kQueueMaxItems - 1) / kQueueMaxItems) *
+                          (int64_t)b->pairs[0]->passes.size();
+        } else {
+            const int rc = batch_queue_enqueue(b, s);
+            if (rc != OPIV_OK) {
+                cudaStreamSynchronize(s);
+                return done(rc);
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            const opiv_plan* pl = b->pairs[i]->passes.back();
+            CUDA_TRY_D(cudaMemcpyAsync(out_vec[i], pl->d_vec, sizeof(opiv_vector) * pl->n_win,
+                                       cudaMemcpyDeviceToHost, s));
+            if (out_peak)
+                CUDA_TRY_D(cudaMemcpyAsync(out_peak[i], pl->d_peak, sizeof(int32_t) * pl->n_win,
+                                           cudaMemcpyDeviceToHost, s));
+        }
+        CUDA_TRY_D(cudaStreamSynchronize(s));
+        return done(OPIV_OK);
     }
     // work already queued on the batch's stream comes first
     const int ns = (int)b->streams.size();

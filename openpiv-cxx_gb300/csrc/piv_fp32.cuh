@@ -217,9 +217,10 @@ __host__ __device__ constexpr int group_smem_float2() { return W * (W + 1) + W *
 // Transform stages of a pair, run by one runtime loop around one FFT body.
 enum { kStLoad0 = 0, kStCol0 = 1, kStLoad1 = 2, kStCol1 = 3, kStInvA = 4, kStInvB = 5 };
 
+// One task: the 2 * NG windows first = task * 2 * NG ... of pair p, run by
+// the calling warp (its lane groups' shared memory at `dyn_smem`).
 template <int W, int MODE, bool LIMIT, typename PixT, bool PLANES, bool VEC>
-__global__ void __launch_bounds__(32 * kWarps, 4)
-piv_fp32_kernel(const PivParams p)
+__device__ __forceinline__ void fp32_task(const PivParams& p, const int task, float2* dyn_smem)
 {
     constexpr int NG = 32 / W;          // lane groups per warp
     constexpr int N = W * W;
@@ -230,13 +231,10 @@ piv_fp32_kernel(const PivParams p)
     constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
 
-    extern __shared__ float2 dyn_smem[];
-
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int grp = lane / W;
     const int gl = lane % W;
-    const int task = blockIdx.x * kWarps + warp;
     const int first = task * 2 * NG;
     if (first >= (int)p.n_win) return;   // warp-uniform
     float2* S = dyn_smem + (warp * NG + grp) * group_smem_float2<W>();   // transpose tile
@@ -493,8 +491,69 @@ piv_fp32_kernel(const PivParams p)
                 p.out_disp[w] = has2 ? pack_disp(px - W / 2 + ox, py - W / 2 + oy) : pack_disp(ox, oy);
             if (!certain && p.flag_list) {
                 const unsigned int slot = atomicAdd(p.flag_count, 1u);
-                p.flag_list[slot] = (int32_t)w;
+                p.flag_list[slot] = (int32_t)w + p.flag_base;
             }
+        }
+    }
+}
+
+extern __shared__ float2 fp32_dyn_smem[];
+
+template <int W, int MODE, bool LIMIT, typename PixT, bool PLANES, bool VEC>
+__global__ void __launch_bounds__(32 * kWarps, 4)
+piv_fp32_kernel(const PivParams p)
+{
+    fp32_task<W, MODE, LIMIT, PixT, PLANES, VEC>(p, (int)blockIdx.x * kWarps + (int)(threadIdx.x >> 5),
+                                                 fp32_dyn_smem);
+}
+
+// Copies pair j's descriptor from global memory into `dst` (shared) with
+// the lanes of one warp; the warp's lanes then read it from there.
+__device__ __forceinline__ const PivParams& warp_item(const PivQueue& q, int j, PivParams* dst)
+{
+    constexpr int NQ = (int)(sizeof(PivParams) / 16);
+    const uint4* src = reinterpret_cast<const uint4*>(q.items_g + j);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < NQ; i += 32) d[i] = __ldg(src + i);
+    __syncwarp();
+    return *dst;
+}
+
+// Persistent form over a device work queue: each CTA takes kWarps * q.chunk
+// consecutive tasks at a time, its warps interleaved over them (so that, as
+// in the single-pair kernel, the warps of a CTA work on neighbouring
+// windows, which share image rows in L1), until the pass's tasks (every
+// pair's) run out.  The next chunk is claimed while the current one runs
+// (thread 0 keeps the atomic's result in a register until the next
+// barrier), so no CTA stalls on the counter.  No CTA waits for another.
+template <int W, int MODE, bool LIMIT, typename PixT, bool VEC>
+__global__ void __launch_bounds__(32 * kWarps, 4)
+piv_fp32_queue_kernel(const __grid_constant__ PivQueue q)
+{
+    __shared__ unsigned int s_t0;
+    __shared__ __align__(16) unsigned char s_items[kWarps * sizeof(PivParams)];
+    const int warp = threadIdx.x >> 5;
+    PivParams* my_item = reinterpret_cast<PivParams*>(s_items) + warp;
+    const int n_tasks = q.first_task[q.n_items];
+    const int step = kWarps * q.chunk;
+    unsigned int next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(q.head, (unsigned int)step);
+#pragma unroll 1
+    for (;;) {
+        if (threadIdx.x == 0) s_t0 = next;
+        __syncthreads();
+        const unsigned int t0 = s_t0;
+        __syncthreads();   // every thread has read s_t0 before it is written again
+        if (t0 >= (unsigned int)n_tasks) break;
+        if (threadIdx.x == 0) next = atomicAdd(q.head, (unsigned int)step);
+        const int t1 = min((int)t0 + step, n_tasks);
+#pragma unroll 1
+        for (int t = (int)t0 + warp; t < t1; t += kWarps) {
+            const int j = __ldg(q.task_item + t);
+            const PivParams& p = warp_item(q, j, my_item);
+            fp32_task<W, MODE, LIMIT, PixT, false, VEC>(p, t - q.first_task[j], fp32_dyn_smem);
+            __syncwarp();   // the descriptor is overwritten by the next task
         }
     }
 }
@@ -554,6 +613,81 @@ cudaError_t launch_w(const PivParams& p, int dtype, int mode, int limit, bool pl
                      : launch_dt<W, kModeComplex, false>(p, dtype, planes, s);
     return limit ? launch_dt<W, kModeReal, true>(p, dtype, planes, s)
                  : launch_dt<W, kModeReal, false>(p, dtype, planes, s);
+}
+
+// The same work list dispatched by the hardware: CTA b runs tasks
+// kWarps * b ... (one per warp), no persistent loop.
+template <int W, int MODE, bool LIMIT, typename PixT, bool VEC>
+__global__ void __launch_bounds__(32 * kWarps, 4)
+piv_fp32_list_kernel(const __grid_constant__ PivQueue q)
+{
+    __shared__ __align__(16) unsigned char s_items[kWarps * sizeof(PivParams)];
+    const int warp = threadIdx.x >> 5;
+    const int t = (int)blockIdx.x * kWarps + warp;
+    if (t >= q.first_task[q.n_items]) return;   // warp-uniform
+    const int j = __ldg(q.task_item + t);
+    const PivParams& p = warp_item(q, j, reinterpret_cast<PivParams*>(s_items) + warp);
+    fp32_task<W, MODE, LIMIT, PixT, false, VEC>(p, t - q.first_task[j], fp32_dyn_smem);
+}
+
+// ---- the persistent queue form ------------------------------------------------
+// blocks > 0: the persistent kernel on `blocks` CTAs; blocks == 0: the
+// hardware-dispatched list kernel, one CTA per kWarps tasks
+template <int W, int MODE, bool LIMIT, typename PixT, bool VEC>
+cudaError_t queue_t(const PivQueue& q, int blocks, int* max_ctas, cudaStream_t s)
+{
+    constexpr int NG = 32 / W;
+    const size_t smem = sizeof(float2) * kWarps * NG * group_smem_float2<W>();
+    auto kern = piv_fp32_queue_kernel<W, MODE, LIMIT, PixT, VEC>;
+    auto list = piv_fp32_list_kernel<W, MODE, LIMIT, PixT, VEC>;
+    static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(list, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_done.fetch_or(bit);
+    }
+    if (max_ctas) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(max_ctas, kern, 32 * kWarps, smem);
+    if (blocks < 0) return cudaErrorInvalidValue;
+    if (blocks == 0) {
+        const int n_tasks = q.first_task[q.n_items];
+        if (n_tasks <= 0) return cudaSuccess;
+        list<<<(unsigned)((n_tasks + kWarps - 1) / kWarps), 32 * kWarps, smem, s>>>(q);
+    } else {
+        kern<<<(unsigned)blocks, 32 * kWarps, smem, s>>>(q);
+    }
+    return cudaGetLastError();
+}
+
+template <int W, int MODE, bool LIMIT>
+cudaError_t queue_dt(const PivQueue& q, int dtype, bool vec, int blocks, int* max_ctas, cudaStream_t s)
+{
+    switch (dtype) {
+    case kU8: return vec ? queue_t<W, MODE, LIMIT, uint8_t, true>(q, blocks, max_ctas, s)
+                         : queue_t<W, MODE, LIMIT, uint8_t, false>(q, blocks, max_ctas, s);
+    case kU16: return vec ? queue_t<W, MODE, LIMIT, uint16_t, true>(q, blocks, max_ctas, s)
+                          : queue_t<W, MODE, LIMIT, uint16_t, false>(q, blocks, max_ctas, s);
+    case kF32: return vec ? queue_t<W, MODE, LIMIT, float, true>(q, blocks, max_ctas, s)
+                          : queue_t<W, MODE, LIMIT, float, false>(q, blocks, max_ctas, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// Launches the queue kernel (max_ctas null) or reports its resident CTAs
+// per SM in *max_ctas (nothing launched).
+template <int W>
+cudaError_t queue_w(const PivQueue& q, int dtype, int mode, int limit, bool vec, int blocks,
+                    int* max_ctas, cudaStream_t s)
+{
+    if (mode == kModeComplex)
+        return limit ? queue_dt<W, kModeComplex, true>(q, dtype, vec, blocks, max_ctas, s)
+                     : queue_dt<W, kModeComplex, false>(q, dtype, vec, blocks, max_ctas, s);
+    return limit ? queue_dt<W, kModeReal, true>(q, dtype, vec, blocks, max_ctas, s)
+                 : queue_dt<W, kModeReal, false>(q, dtype, vec, blocks, max_ctas, s);
 }
 
 }  // namespace fp32

@@ -161,16 +161,18 @@ __device__ __forceinline__ float block_sum(float v, float* red)
     return s;
 }
 
+extern __shared__ float2 w64_dyn_smem[];
+
+// One task: windows 2 blk and 2 blk + 1 of pair p, run by the whole CTA.
 template <int MODE, bool LIMIT, typename PixT, bool PLANES>
-__global__ void __launch_bounds__(kThreads, 3)
-piv_w64_kernel(const PivParams p)
+__device__ __forceinline__ void w64_task(const PivParams& p, const int blk)
 {
     constexpr int D0 = LIMIT ? W / 4 : 0;
     constexpr int VW = LIMIT ? W / 2 : W;
     constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
 
-    extern __shared__ float2 sm[];
+    float2* sm = w64_dyn_smem;
     float2* T1 = sm;                  // first window, then Q, then both planes
     float2* T2 = sm + W * LD;         // second window
     __shared__ float2 tw[64];
@@ -180,7 +182,7 @@ piv_w64_kernel(const PivParams p)
     __shared__ float sped[2];
 
     const int t = threadIdx.x;
-    const int w0 = 2 * blockIdx.x;
+    const int w0 = 2 * blk;
     if (w0 >= (int)p.n_win) return;
     const int w1 = w0 + 1;
     const bool valid1 = w1 < (int)p.n_win;
@@ -408,11 +410,62 @@ piv_w64_kernel(const PivParams p)
                 }
                 if (!certain && p.flag_list) {
                     const unsigned int slot = atomicAdd(p.flag_count, 1u);
-                    p.flag_list[slot] = (int32_t)w;
+                    p.flag_list[slot] = (int32_t)w + p.flag_base;
                 }
             }
         }
         __syncthreads();
+    }
+}
+
+template <int MODE, bool LIMIT, typename PixT, bool PLANES>
+__global__ void __launch_bounds__(kThreads, 3)
+piv_w64_kernel(const PivParams p)
+{
+    w64_task<MODE, LIMIT, PixT, PLANES>(p, (int)blockIdx.x);
+}
+
+// Persistent form over a device work queue: each CTA takes q.chunk tasks
+// (window pairs) at a time until the pass's tasks (every image pair's) run
+// out, claiming the next chunk while the current one runs (thread 0 keeps
+// the atomic's result in a register until the next barrier).  No CTA waits
+// for another.
+// Copies pair j's descriptor from global memory into `dst` (shared) with
+// the CTA's threads; all threads then read it from there.
+__device__ __forceinline__ const PivParams& cta_item(const PivQueue& q, int j, PivParams* dst)
+{
+    constexpr int NQ = (int)(sizeof(PivParams) / 16);
+    const uint4* src = reinterpret_cast<const uint4*>(q.items_g + j);
+    if ((int)threadIdx.x < NQ) reinterpret_cast<uint4*>(dst)[threadIdx.x] = __ldg(src + threadIdx.x);
+    __syncthreads();
+    return *dst;
+}
+
+template <int MODE, bool LIMIT, typename PixT>
+__global__ void __launch_bounds__(kThreads, 3)
+piv_w64_queue_kernel(const __grid_constant__ PivQueue q)
+{
+    __shared__ unsigned int s_t0;
+    __shared__ __align__(16) unsigned char s_item[sizeof(PivParams)];
+    const int n_tasks = q.first_task[q.n_items];
+    unsigned int next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(q.head, (unsigned int)q.chunk);
+#pragma unroll 1
+    for (;;) {
+        if (threadIdx.x == 0) s_t0 = next;
+        __syncthreads();
+        const unsigned int t0 = s_t0;
+        __syncthreads();   // every thread has read s_t0 before it is written again
+        if (t0 >= (unsigned int)n_tasks) break;
+        if (threadIdx.x == 0) next = atomicAdd(q.head, (unsigned int)q.chunk);
+        const int t1 = min((int)t0 + q.chunk, n_tasks);
+#pragma unroll 1
+        for (int t = (int)t0; t < t1; ++t) {
+            const int j = __ldg(q.task_item + t);
+            // the task ends with a barrier: the previous descriptor is no longer read
+            const PivParams& p = cta_item(q, j, reinterpret_cast<PivParams*>(s_item));
+            w64_task<MODE, LIMIT, PixT, false>(p, t - q.first_task[j]);
+        }
     }
 }
 
@@ -448,7 +501,73 @@ cudaError_t launch_dt(const PivParams& p, int dtype, bool planes, cudaStream_t s
     }
 }
 
+// The same work list dispatched by the hardware: CTA b runs task b, no
+// persistent loop.
+template <int MODE, bool LIMIT, typename PixT>
+__global__ void __launch_bounds__(kThreads, 3)
+piv_w64_list_kernel(const __grid_constant__ PivQueue q)
+{
+    __shared__ __align__(16) unsigned char s_item[sizeof(PivParams)];
+    const int t = (int)blockIdx.x;
+    const int j = __ldg(q.task_item + t);
+    const PivParams& p = cta_item(q, j, reinterpret_cast<PivParams*>(s_item));
+    w64_task<MODE, LIMIT, PixT, false>(p, t - q.first_task[j]);
+}
+
+// blocks > 0: the persistent kernel on `blocks` CTAs; blocks == 0: the
+// hardware-dispatched list kernel, one CTA per task
+template <int MODE, bool LIMIT, typename PixT>
+cudaError_t queue_t(const PivQueue& q, int blocks, int* max_ctas, cudaStream_t s)
+{
+    const size_t smem = sizeof(float2) * 2 * W * LD;
+    auto kern = piv_w64_queue_kernel<MODE, LIMIT, PixT>;
+    auto list = piv_w64_list_kernel<MODE, LIMIT, PixT>;
+    static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(list, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_done.fetch_or(bit);
+    }
+    if (max_ctas) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(max_ctas, kern, kThreads, smem);
+    if (blocks < 0) return cudaErrorInvalidValue;
+    if (blocks == 0) {
+        const int n_tasks = q.first_task[q.n_items];
+        if (n_tasks <= 0) return cudaSuccess;
+        list<<<(unsigned)n_tasks, kThreads, smem, s>>>(q);
+    } else {
+        kern<<<(unsigned)blocks, kThreads, smem, s>>>(q);
+    }
+    return cudaGetLastError();
+}
+
+template <int MODE, bool LIMIT>
+cudaError_t queue_dt(const PivQueue& q, int dtype, int blocks, int* max_ctas, cudaStream_t s)
+{
+    switch (dtype) {
+    case kU8: return queue_t<MODE, LIMIT, uint8_t>(q, blocks, max_ctas, s);
+    case kU16: return queue_t<MODE, LIMIT, uint16_t>(q, blocks, max_ctas, s);
+    case kF32: return queue_t<MODE, LIMIT, float>(q, blocks, max_ctas, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace w64
+
+// the 64 px kernel loads rows element-wise and needs no alignment flag
+cudaError_t queue_piv_fp32_w64(const PivQueue& q, int dtype, int mode, int limit, bool, int blocks,
+                               int* max_ctas, cudaStream_t s)
+{
+    if (mode == kModeComplex)
+        return limit ? w64::queue_dt<kModeComplex, true>(q, dtype, blocks, max_ctas, s)
+                     : w64::queue_dt<kModeComplex, false>(q, dtype, blocks, max_ctas, s);
+    return limit ? w64::queue_dt<kModeReal, true>(q, dtype, blocks, max_ctas, s)
+                 : w64::queue_dt<kModeReal, false>(q, dtype, blocks, max_ctas, s);
+}
 
 cudaError_t launch_piv_fp32_w64(const PivParams& p, int dtype, int mode, int limit, bool planes,
                                 cudaStream_t s)

@@ -25,6 +25,7 @@ struct PivParams {
     // windows whose FP32 decisions are not certain (see piv_fp32.cu)
     unsigned int* flag_count = nullptr;
     int32_t* flag_list = nullptr;
+    int32_t flag_base = 0;             // added to a flagged window's index (a queue's list)
     float kappa = 16.f;                // FP32 error-bound factor
     // debug / per-window API outputs
     float* planes = nullptr;           // FP32 kernel: n_win * W * W (mean-free part)
@@ -90,6 +91,63 @@ inline cudaError_t launch_piv_fp32(const PivParams& p, int w, int dtype, int mod
 bool exact_supports(int w);
 cudaError_t launch_piv_exact(const PivParams& p, int w, int dtype, int mode, int limit,
                              bool use_list, int blocks, cudaStream_t s);
+
+// Device work queue of one pass over up to kQueueMaxItems image pairs (one
+// window size), passed by value in the kernel's parameter space (read
+// through the constant cache): pair j is items[j]; its tasks are numbered
+// first_task[j] .. first_task[j + 1] - 1 and its windows first_win[j] ..
+// first_win[j + 1] - 1 in the queue's combined numbering.  A persistent
+// grid takes tasks from *head (zero before the launch); a task is what one
+// warp (16, 32 px: 2 * 32 / W windows) or one CTA (64 px: two windows) of
+// the single-pair kernel does.  Every item flags its uncertain windows into
+// one list (flag_count / flag_list, combined window numbers), which the
+// exact queue kernel then re-decides for all the queue's pairs at once.
+constexpr int kQueueMaxItems = 64;
+struct PivQueue {
+    PivParams items[kQueueMaxItems];
+    int first_task[kQueueMaxItems + 1] = {};
+    int first_win[kQueueMaxItems + 1] = {};
+    int n_items = 0;
+    // the same descriptors in global memory (a task copies its pair's into
+    // shared memory) and the pair of every task, one byte each
+    const PivParams* items_g = nullptr;
+    const uint8_t* task_item = nullptr;
+    unsigned int* head = nullptr;
+    int chunk = 1;
+    const unsigned int* flag_count = nullptr;
+    const int32_t* flag_list = nullptr;
+};
+static_assert(kQueueMaxItems <= 256, "task_item holds pair numbers in one byte");
+static_assert(sizeof(PivParams) % 16 == 0, "descriptors are copied in 16-byte words");
+// tasks of a pair of n_win windows in the queue of window size w
+inline int fp32_queue_tasks(int w, int64_t n_win)
+{
+    const int per = w == 64 ? 2 : 2 * (32 / w);
+    return (int)((n_win + per - 1) / per);
+}
+// Queue kernels per window size (piv_fp32_w*.cu).  `vec`: every item's A
+// rows start on 16-byte boundaries (128-bit loads); `blocks` CTAs of the
+// persistent grid.  With max_ctas non-null nothing is launched and
+// *max_ctas receives the kernel's resident CTAs per SM.
+cudaError_t queue_piv_fp32_w16(const PivQueue& q, int dtype, int mode, int limit, bool vec, int blocks,
+                               int* max_ctas, cudaStream_t s);
+cudaError_t queue_piv_fp32_w32(const PivQueue& q, int dtype, int mode, int limit, bool vec, int blocks,
+                               int* max_ctas, cudaStream_t s);
+cudaError_t queue_piv_fp32_w64(const PivQueue& q, int dtype, int mode, int limit, bool vec, int blocks,
+                               int* max_ctas, cudaStream_t s);
+inline cudaError_t queue_piv_fp32(const PivQueue& q, int w, int dtype, int mode, int limit, bool vec,
+                                  int blocks, int* max_ctas, cudaStream_t s)
+{
+    if (w == 16) return queue_piv_fp32_w16(q, dtype, mode, limit, vec, blocks, max_ctas, s);
+    if (w == 32) return queue_piv_fp32_w32(q, dtype, mode, limit, vec, blocks, max_ctas, s);
+    if (w == 64) return queue_piv_fp32_w64(q, dtype, mode, limit, vec, blocks, max_ctas, s);
+    return cudaErrorInvalidValue;
+}
+// The exact pass over a queue's combined flag list (piv_exact.cu), and the
+// resident CTAs per SM of that kernel for window size w.
+cudaError_t launch_piv_exact_queue(const PivQueue& q, int w, int dtype, int mode, int limit,
+                                   int blocks, cudaStream_t s);
+int exact_queue_max_ctas_per_sm(int w);
 
 // Records `message` as the calling thread's last error (opiv_last_error)
 // and returns `status`.

@@ -56,7 +56,10 @@ SYMBOLS = [
     "opiv_batch_upload", "opiv_batch_run", "opiv_batch_window_count", "opiv_batch_results",
     "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
     "opiv_process_pairs", "opiv_plan_adjoint", "opiv_batch_process", "opiv_plan_create_tc",
+    "opiv_batch_set_schedule", "opiv_batch_set_tuning", "opiv_batch_get_tuning",
+    "opiv_batch_autotune",
 ]
+BATCH_STREAMS, BATCH_QUEUE = 0, 1
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
                          ("v", np.float32), ("sn", np.float32)])
@@ -159,6 +162,10 @@ def load(path: str | None = None) -> C.CDLL:
                                      C.c_void_p]
     L.opiv_batch_process.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                      C.POINTER(C.c_size_t), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+    L.opiv_batch_set_schedule.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_batch_set_tuning.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+    L.opiv_batch_get_tuning.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, C.POINTER(C.c_float)]
+    L.opiv_batch_autotune.argtypes = [C.c_void_p, C.c_void_p]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -424,6 +431,25 @@ class Batch:
 
     def run(self, use_graph: bool = True, stream: int = 0):
         _check(load().opiv_batch_run(self._h, int(bool(use_graph)), stream or None))
+
+    def set_schedule(self, schedule: int):
+        """BATCH_STREAMS (per-pair pass chains on fork streams) or BATCH_QUEUE
+        (per pass one persistent kernel over a device work queue of all pairs)."""
+        _check(load().opiv_batch_set_schedule(self._h, schedule))
+
+    def set_tuning(self, k: int, ctas_per_sm: int, chunk: int):
+        _check(load().opiv_batch_set_tuning(self._h, k, ctas_per_sm, chunk))
+
+    def tuning(self, k: int):
+        """(CTAs per SM, tasks per warp and dequeue, resident CTA limit, the
+        autotuner's fastest pass time in ms or 0) of pass k's queue."""
+        c, ch, mx, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
+        _check(load().opiv_batch_get_tuning(self._h, k, C.byref(c), C.byref(ch), C.byref(mx), C.byref(ms)))
+        return c.value, ch.value, mx.value, ms.value
+
+    def autotune(self, stream: int = 0):
+        """Queue schedule; each pass's grid and chunk timed on the frames held now."""
+        _check(load().opiv_batch_autotune(self._h, stream or None))
 
     def process_into(self, ptrs_a, ptrs_b, pitches, ptrs_vec, ptrs_peak=None):
         """Host pointers, one per pair (pinned for overlap): every pair's

@@ -1,6 +1,7 @@
 """C ABI checks that need no GPU: the library loads, exports every symbol the
 header declares, and its host-side parts (grids, argument validation, the
 host find_peaks / fit_simple_gaussian) agree with the oracle."""
+import ctypes
 import json
 import os
 import re
@@ -122,3 +123,15 @@ def test_host_find_peaks_and_fit(lib, orc):
                               orc.fit_simple_gaussian(plane, px, py))
     with pytest.raises(og.OpivError):
         og.fit_simple_gaussian(np.ones((32, 32)), 0, 5)
+
+
+def test_batch_schedule_calls_check_arguments(lib):
+    """The queue-schedule calls of a batch reject a null batch before they
+    touch a device."""
+    L = og.load()
+    a, b, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    assert L.opiv_batch_set_schedule(None, og.BATCH_QUEUE) == og.ERR_ARG
+    assert L.opiv_batch_set_tuning(None, 0, 1, 1) == og.ERR_ARG
+    assert L.opiv_batch_get_tuning(None, 0, ctypes.byref(a), ctypes.byref(b), ctypes.byref(m), None) == og.ERR_ARG
+    assert L.opiv_batch_autotune(None, None) == og.ERR_ARG
+    assert "null" in L.opiv_last_error().decode()
