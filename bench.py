@@ -510,6 +510,7 @@ def run_batch(args):
     batch.autotune(stream=h)
     t_tune = time.perf_counter() - t_tune
     tuning = [batch.tuning(k) for k in range(n_pass)]
+    lanes = batch.lanes()
     for _ in range(args.warmup):
         batch.run(use_graph=True, stream=h)
     launches_before = og.kernel_launch_count()
@@ -592,7 +593,7 @@ def run_batch(args):
             "launches_per_step": {"streams": launches_streams / args.steps,
                                   "queue": launches_queue / args.steps},
             "exact_windows_per_pass": exact_per_pass,
-            "autotune": {"seconds": t_tune,
+            "autotune": {"seconds": t_tune, "lanes": lanes,
                          "per_pass": [{"ia": BATCH_PASSES[k][0], "ctas_per_sm": c, "chunk": ch,
                                        "resident_limit": mx, "pass_ms": ms}
                                       for k, (c, ch, mx, ms) in enumerate(tuning)]},

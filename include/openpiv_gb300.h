@@ -278,11 +278,12 @@ int opiv_batch_process(opiv_batch* batch, const void* const* frames_a, const voi
 /* Schedules of a batch (no counterpart in the reference).
  * OPIV_BATCH_STREAMS (the default): every pair's pass chain on a fork
  *   stream, two launches per pair and pass.
- * OPIV_BATCH_QUEUE: per pass and group of up to 64 pairs, one persistent
- *   kernel over a device work queue that holds the group's windows (CTAs
- *   take tasks from an atomic counter; no kernel waits on another), then one
- *   exact re-decision launch over the group's flagged windows: two launches
- *   per pass for batches of up to 64 pairs.  Results are identical to the
+ * OPIV_BATCH_QUEUE: per pass and group of up to 64 pairs, one launch over
+ *   a device work list that holds the group's windows (a persistent grid
+ *   whose CTAs take tasks from an atomic counter, or one CTA per task group;
+ *   see the tuning), then one exact re-decision launch over the group's
+ *   flagged windows; the groups form lanes on fork streams (see
+ *   opiv_batch_set_lanes).  Results are identical to the
  *   streams schedule.  Window sizes 16, 32 and 64 (the FP32 kernels);
  *   OPIV_ERR_UNSUPPORTED otherwise, and when a group's combined window
  *   count exceeds 2^31 - 1.  opiv_batch_process under this schedule uploads
@@ -307,13 +308,23 @@ int opiv_batch_set_tuning(opiv_batch* batch, int pass, int ctas_per_sm, int chun
  * when the pass's tuning did not come from the autotuner). */
 int opiv_batch_get_tuning(const opiv_batch* batch, int pass, int* ctas_per_sm, int* chunk,
                           int* max_ctas_per_sm, float* tuned_ms);
+/* Lanes of the queue schedule (1 .. 8, default 2, at most the number of
+ * pairs): the pairs are split into `lanes` sets of about equal image area,
+ * each running its pass chain on its own fork stream, so that one lane's
+ * exact re-decision (a few hundred microseconds of FP64 latency per pass)
+ * overlaps another lane's FP32 kernel.  Two launches per pass and group;
+ * a group holds up to 64 pairs of one lane.  opiv_batch_get_lanes returns
+ * the lanes in use (or a negative status). */
+int opiv_batch_set_lanes(opiv_batch* batch, int lanes);
+int opiv_batch_get_lanes(const opiv_batch* batch);
 /* Autotuner: selects the queue schedule and, pass after pass, times every
  * candidate (the hardware-dispatched list; persistent grids of 1 .. resident
  * limit (at most 4) CTAs per SM with chunk 1, 2, 4, 8; fastest of
  * two timed runs after one warm-up, CUDA events on `stream`) on the frames
  * the batch holds now, and keeps the fastest per pass.  The pass chain runs
- * in order, so each pass is tuned on the real offsets of the one before;
- * the batch's results afterwards are those of a normal run.  Synchronous. */
+ * in order, so each pass is tuned on the real offsets of the one before.
+ * Then the whole chain is timed with 1 and 2 lanes and the faster kept.
+ * The batch's results afterwards are those of a normal run.  Synchronous. */
 int opiv_batch_autotune(opiv_batch* batch, void* stream);
 
 /* ---- allocation-free pass ------------------------------------------------ */

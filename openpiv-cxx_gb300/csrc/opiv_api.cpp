@@ -847,7 +847,14 @@ struct opiv_batch {
     int schedule = OPIV_BATCH_STREAMS;
     std::vector<batch_queue_pass> qp;
     std::vector<int> tune_ctas, tune_chunk;
+    std::vector<float> tune_ms;
     int sms = 0;
+    // lanes of the queue schedule: the pairs split into `lanes` sets of about
+    // equal area, each running its pass chain on its own fork stream; groups
+    // are ordered lane by lane, lane l owning groups lane_first[l] ..
+    // lane_first[l + 1] - 1
+    int lanes = 2;
+    std::vector<int> lane_first;
 };
 
 namespace {
@@ -878,8 +885,31 @@ int batch_queue_setup(opiv_batch* b)
     if (!b->qp.empty()) return OPIV_OK;
     const int n = (int)b->pairs.size();
     const int n_pass = (int)b->pairs[0]->passes.size();
-    const int n_groups = (n + kQueueMaxItems - 1) / kQueueMaxItems;
     if (b->sms == 0) CUDA_TRY(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
+    // pairs to lanes, largest image first to the lane with the least area;
+    // each lane's pairs (in index order) in groups of up to kQueueMaxItems
+    const int L = std::max(1, std::min({ b->lanes, n, (int)b->streams.size() }));
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    auto area = [&](int i) { return (int64_t)b->pairs[i]->passes[0]->img_w * b->pairs[i]->passes[0]->img_h; };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return area(x) > area(y); });
+    std::vector<std::vector<int>> lane_pairs(L);
+    std::vector<int64_t> load(L, 0);
+    for (int i : order) {
+        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        lane_pairs[l].push_back(i);
+        load[l] += area(i);
+    }
+    std::vector<std::vector<int>> group_pairs;
+    b->lane_first.assign(1, 0);
+    for (int l = 0; l < L; ++l) {
+        std::sort(lane_pairs[l].begin(), lane_pairs[l].end());
+        for (size_t i0 = 0; i0 < lane_pairs[l].size(); i0 += kQueueMaxItems)
+            group_pairs.emplace_back(lane_pairs[l].begin() + i0,
+                                     lane_pairs[l].begin() + std::min(lane_pairs[l].size(), i0 + kQueueMaxItems));
+        b->lane_first.push_back((int)group_pairs.size());
+    }
+    const int n_groups = (int)group_pairs.size();
     std::vector<batch_queue_pass> qs(n_pass);
     int rc = OPIV_OK;
     for (int k = 0; k < n_pass && rc == OPIV_OK; ++k) {
@@ -900,18 +930,18 @@ int batch_queue_setup(opiv_batch* b)
         const size_t px = px_bytes(q.dtype);
         for (int g = 0; g < n_groups && rc == OPIV_OK; ++g) {
             PivQueue& pq = q.groups[g];
-            const int i0 = g * kQueueMaxItems, i1 = std::min(n, i0 + kQueueMaxItems);
-            pq.n_items = i1 - i0;
+            pq.n_items = (int)group_pairs[g].size();
             int64_t tasks = 0, wins = 0;
-            for (int i = i0; i < i1; ++i) {
+            for (int j = 0; j < pq.n_items; ++j) {
+                const int i = group_pairs[g][j];
                 const opiv_plan* p = b->pairs[i]->passes[k];
                 const opiv_plan* prev = k ? b->pairs[i]->passes[k - 1] : nullptr;
                 PivParams it = pass_params(p, b->d_fa[i], b->d_fb[i], b->pitch[i], p->d_vec, p->d_peak, prev);
-                pq.first_task[i - i0] = (int)tasks;
-                pq.first_win[i - i0] = (int)wins;
+                pq.first_task[j] = (int)tasks;
+                pq.first_win[j] = (int)wins;
                 it.flag_base = (int32_t)wins;
                 const int nt = fp32_queue_tasks(q.ia, p->n_win);
-                task_item.insert(task_item.end(), (size_t)nt, (uint8_t)(i - i0));
+                task_item.insert(task_item.end(), (size_t)nt, (uint8_t)j);
                 tasks += nt;
                 wins += p->n_win;
                 if (tasks > INT32_MAX || wins > INT32_MAX) {
@@ -923,7 +953,7 @@ int batch_queue_setup(opiv_batch* b)
                 q.vec = q.vec && ((uintptr_t)it.fa % 16 == 0) && ((uintptr_t)it.fb % 16 == 0) &&
                         (it.pitch % 16 == 0) && (((size_t)it.gx0 * px) % 16 == 0) &&
                         (((size_t)it.gdx * px) % 16 == 0) && (((size_t)q.ia * px) % 16 == 0);
-                pq.items[i - i0] = it;
+                pq.items[j] = it;
             }
             pq.first_task[pq.n_items] = (int)tasks;
             pq.first_win[pq.n_items] = (int)wins;
@@ -973,6 +1003,7 @@ int batch_queue_setup(opiv_batch* b)
         q.exact_blocks = exact_queue_max_ctas_per_sm(q.ia) * b->sms;
         q.ctas_per_sm = b->tune_ctas[k];
         q.chunk = b->tune_chunk[k];
+        q.tuned_ms = b->tune_ms[k];
     }
     b->qp.swap(qs);
     if (rc != OPIV_OK) batch_free_queue(b);   // a failed set-up's partial buffers
@@ -982,13 +1013,15 @@ int batch_queue_setup(opiv_batch* b)
 // Pass k of the queue schedule on stream s: counters reset, then per group
 // of pairs the persistent FP32 kernel and the exact re-decision of the
 // group's flagged windows.
-int batch_queue_pass_enqueue(opiv_batch* b, int k, cudaStream_t s)
+int batch_queue_pass_enqueue(opiv_batch* b, int k, cudaStream_t s, int g0 = 0, int g1 = -1)
 {
     batch_queue_pass& q = b->qp[k];
+    if (g1 < 0) g1 = (int)q.groups.size();
     // CTAs of the persistent grid; 0: the hardware-dispatched list kernel
     const int ctas = q.ctas_per_sm >= 0 ? q.ctas_per_sm : q.max_ctas;
-    CUDA_TRY(cudaMemsetAsync(q.d_ctr, 0, 2 * sizeof(unsigned int) * q.groups.size(), s));
-    for (PivQueue& pq : q.groups) {
+    CUDA_TRY(cudaMemsetAsync(q.d_ctr + 2 * g0, 0, 2 * sizeof(unsigned int) * (g1 - g0), s));
+    for (int g = g0; g < g1; ++g) {
+        PivQueue& pq = q.groups[g];
         pq.chunk = q.chunk;
         CUDA_TRY(queue_piv_fp32(pq, q.ia, q.dtype, q.mode, q.limit, q.vec, ctas * b->sms, nullptr, s));
         ++g_launches;
@@ -998,11 +1031,35 @@ int batch_queue_pass_enqueue(opiv_batch* b, int k, cudaStream_t s)
     return OPIV_OK;
 }
 
+// The whole chain: one lane on s; several lanes forked from s onto the
+// batch's streams, each running all passes of its pairs, joined back into s
+// (one lane's exact pass overlaps another lane's FP32 kernel).
 int batch_queue_enqueue(opiv_batch* b, cudaStream_t s)
 {
     int rc = batch_queue_setup(b);
-    for (int k = 0; k < (int)b->qp.size() && rc == OPIV_OK; ++k) rc = batch_queue_pass_enqueue(b, k, s);
+    if (rc != OPIV_OK) return rc;
+    const int L = (int)b->lane_first.size() - 1;
+    if (L <= 1) {
+        for (int k = 0; k < (int)b->qp.size() && rc == OPIV_OK; ++k) rc = batch_queue_pass_enqueue(b, k, s);
+        return rc;
+    }
+    const int ns = (int)b->streams.size();
+    CUDA_TRY(cudaEventRecord(b->events[ns], s));
+    for (int l = 0; l < L; ++l) CUDA_TRY(cudaStreamWaitEvent(b->streams[l], b->events[ns], 0));
+    for (int k = 0; k < (int)b->qp.size() && rc == OPIV_OK; ++k)
+        for (int l = 0; l < L && rc == OPIV_OK; ++l)
+            rc = batch_queue_pass_enqueue(b, k, b->streams[l], b->lane_first[l], b->lane_first[l + 1]);
+    for (int l = 0; l < L; ++l) {
+        CUDA_TRY(cudaEventRecord(b->events[l], b->streams[l]));
+        CUDA_TRY(cudaStreamWaitEvent(s, b->events[l], 0));
+    }
     return rc;
+}
+
+int64_t batch_queue_launches(const opiv_batch* b)
+{
+    if (b->qp.empty()) return 0;
+    return 2 * (int64_t)b->qp[0].groups.size() * (int64_t)b->qp.size();
 }
 
 }  // namespace
@@ -1052,6 +1109,7 @@ int opiv_batch_create(opiv_batch** out, int n_pairs, const uint32_t* widths, con
     }
     b->tune_ctas.assign(n_passes, -1);
     b->tune_chunk.assign(n_passes, 1);
+    b->tune_ms.assign(n_passes, 0.f);
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(device);
@@ -1175,9 +1233,8 @@ int opiv_batch_run(opiv_batch* b, int use_graph, void* stream)
         return done(OPIV_OK);   // the eager run has produced this call's results
     }
     if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return done(cuda_fail(e, "cudaGraphLaunch"));
-    const int64_t per_pass = queue ? (int64_t)(b->pairs.size() + kQueueMaxItems - 1) / kQueueMaxItems
-                                   : (int64_t)b->pairs.size();
-    g_launches += 2 * per_pass * (int64_t)b->pairs[0]->passes.size();
+    g_launches += queue ? batch_queue_launches(b)
+                        : 2 * (int64_t)b->pairs.size() * (int64_t)b->pairs[0]->passes.size();
     return done(OPIV_OK);
 }
 
@@ -1205,6 +1262,7 @@ int opiv_batch_set_tuning(opiv_batch* b, int pass, int ctas_per_sm, int chunk)
     if (chunk < 1 || chunk > 1024) return fail(OPIV_ERR_ARG, "chunk %d outside 1 .. 1024", chunk);
     b->tune_ctas[pass] = ctas_per_sm;
     b->tune_chunk[pass] = chunk;
+    b->tune_ms[pass] = 0.f;
     if (!b->qp.empty()) {
         b->qp[pass].ctas_per_sm = ctas_per_sm;
         b->qp[pass].chunk = chunk;
@@ -1230,8 +1288,31 @@ int opiv_batch_get_tuning(const opiv_batch* b, int pass, int* ctas_per_sm, int* 
     *ctas_per_sm = b->tune_ctas[pass] >= 0 ? b->tune_ctas[pass] : mx;
     *chunk = b->tune_chunk[pass];
     if (max_ctas_per_sm) *max_ctas_per_sm = mx;
-    if (tuned_ms) *tuned_ms = b->qp.empty() ? 0.f : b->qp[pass].tuned_ms;
+    if (tuned_ms) *tuned_ms = b->tune_ms[pass];
     return OPIV_OK;
+}
+
+int opiv_batch_set_lanes(opiv_batch* b, int lanes)
+{
+    if (!b) return fail(OPIV_ERR_ARG, "batch is null");
+    if (lanes < 1 || lanes > 8) return fail(OPIV_ERR_ARG, "lanes %d outside 1 .. 8", lanes);
+    if (lanes == b->lanes) return OPIV_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(b->device);
+    cudaStreamSynchronize(b->main);
+    batch_drop_graph(b);
+    batch_free_queue(b);
+    cudaSetDevice(prev);
+    b->lanes = lanes;
+    return OPIV_OK;
+}
+
+int opiv_batch_get_lanes(const opiv_batch* b)
+{
+    if (!b) return fail(OPIV_ERR_ARG, "batch is null");
+    const int n = (int)b->pairs.size();
+    return std::max(1, std::min({ b->lanes, n, (int)b->streams.size() }));
 }
 
 int opiv_batch_autotune(opiv_batch* b, void* stream)
@@ -1292,8 +1373,42 @@ int opiv_batch_autotune(opiv_batch* b, void* stream)
         q.tuned_ms = best;
         b->tune_ctas[k] = best_c;
         b->tune_chunk[k] = best_k;
+        b->tune_ms[k] = best;
         // the pass once more with its choice: the next pass reads its offsets
         rc = batch_queue_pass_enqueue(b, k, s);
+    }
+    // lanes: the whole chain with 1 and 2 lanes (fastest of two timed runs)
+    if (rc == OPIV_OK && b->pairs.size() > 1) {
+        float best = 3.4e38f;
+        int best_l = 1;
+        for (int L = 1; L <= 2 && rc == OPIV_OK; ++L) {
+            b->lanes = L;
+            batch_free_queue(b);
+            float t_min = 3.4e38f;
+            for (int r = 0; r < 3 && rc == OPIV_OK; ++r) {
+                cudaEventRecord(e0, s);
+                rc = batch_queue_enqueue(b, s);
+                cudaEventRecord(e1, s);
+                if (rc != OPIV_OK) break;
+                cudaError_t e = cudaEventSynchronize(e1);
+                if (e != cudaSuccess) {
+                    rc = cuda_fail(e, "autotune run");
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (r > 0 && ms < t_min) t_min = ms;
+            }
+            if (t_min < best) {
+                best = t_min;
+                best_l = L;
+            }
+        }
+        if (rc == OPIV_OK && b->lanes != best_l) {
+            b->lanes = best_l;
+            batch_free_queue(b);
+            rc = batch_queue_enqueue(b, s);   // leaves a normal run's results
+        }
     }
     cudaError_t e = cudaStreamSynchronize(s);
     cudaEventDestroy(e0);
@@ -1347,8 +1462,7 @@ int opiv_batch_process(opiv_batch* b, const void* const* frames_a, const void* c
         }
         if (b->exec) {
             CUDA_TRY_D(cudaGraphLaunch(b->exec, s));
-            g_launches += 2 * (int64_t)((n + kQueueMaxItems - 1) / kQueueMaxItems) *
-                          (int64_t)b->pairs[0]->passes.size();
+            g_launches += batch_queue_launches(b);
         } else {
             const int rc = batch_queue_enqueue(b, s);
             if (rc != OPIV_OK) {

@@ -57,7 +57,7 @@ SYMBOLS = [
     "opiv_plan_set_precision", "opiv_plan_status", "opiv_plan_set_plane_output",
     "opiv_process_pairs", "opiv_plan_adjoint", "opiv_batch_process", "opiv_plan_create_tc",
     "opiv_batch_set_schedule", "opiv_batch_set_tuning", "opiv_batch_get_tuning",
-    "opiv_batch_autotune",
+    "opiv_batch_autotune", "opiv_batch_set_lanes", "opiv_batch_get_lanes",
 ]
 BATCH_STREAMS, BATCH_QUEUE = 0, 1
 
@@ -166,6 +166,8 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_batch_set_tuning.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
     L.opiv_batch_get_tuning.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, C.POINTER(C.c_float)]
     L.opiv_batch_autotune.argtypes = [C.c_void_p, C.c_void_p]
+    L.opiv_batch_set_lanes.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_batch_get_lanes.argtypes = [C.c_void_p]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
     _lib = L
@@ -446,6 +448,13 @@ class Batch:
         c, ch, mx, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
         _check(load().opiv_batch_get_tuning(self._h, k, C.byref(c), C.byref(ch), C.byref(mx), C.byref(ms)))
         return c.value, ch.value, mx.value, ms.value
+
+    def set_lanes(self, lanes: int):
+        """Queue schedule: the pairs split into `lanes` chains on fork streams."""
+        _check(load().opiv_batch_set_lanes(self._h, lanes))
+
+    def lanes(self) -> int:
+        return _check(load().opiv_batch_get_lanes(self._h))
 
     def autotune(self, stream: int = 0):
         """Queue schedule; each pass's grid and chunk timed on the frames held now."""

@@ -134,4 +134,6 @@ def test_batch_schedule_calls_check_arguments(lib):
     assert L.opiv_batch_set_tuning(None, 0, 1, 1) == og.ERR_ARG
     assert L.opiv_batch_get_tuning(None, 0, ctypes.byref(a), ctypes.byref(b), ctypes.byref(m), None) == og.ERR_ARG
     assert L.opiv_batch_autotune(None, None) == og.ERR_ARG
+    assert L.opiv_batch_set_lanes(None, 2) == og.ERR_ARG
+    assert L.opiv_batch_get_lanes(None) == og.ERR_ARG
     assert "null" in L.opiv_last_error().decode()

@@ -69,10 +69,17 @@ def test_queue_schedule_matches_per_pair_multipass(data):
     batch = og.Batch(SIZES, np.uint16, PASSES)
     batch.set_schedule(og.BATCH_QUEUE)
     upload(batch, frames[0])
+    assert batch.lanes() == 2
     n0 = og.kernel_launch_count()
     batch.run(use_graph=False)
-    assert og.kernel_launch_count() - n0 == 2 * len(PASSES)
+    assert og.kernel_launch_count() - n0 == 2 * 2 * len(PASSES)   # two lanes of one group each
     check(batch, expect[0], "queue, default tuning")
+    for lanes in (1, 3, 4, 2):
+        batch.set_lanes(lanes)
+        n0 = og.kernel_launch_count()
+        batch.run(use_graph=False)
+        assert og.kernel_launch_count() - n0 == 2 * lanes * len(PASSES)
+        check(batch, expect[0], f"queue, {lanes} lanes")
     for k in range(len(PASSES)):
         c, ch, mx, ms = batch.tuning(k)
         assert mx >= 1 and c == mx and ch == 1 and ms == 0
@@ -90,7 +97,7 @@ def test_queue_schedule_matches_per_pair_multipass(data):
         upload(batch, frames[j])
         n0 = og.kernel_launch_count()
         batch.run(use_graph=True)
-        assert og.kernel_launch_count() - n0 == 2 * len(PASSES)
+        assert og.kernel_launch_count() - n0 == 2 * 2 * len(PASSES)
         check(batch, expect[j], f"queue, replay {j}")
     # back to the streams schedule: same results
     batch.set_schedule(og.BATCH_STREAMS)
@@ -109,6 +116,7 @@ def test_autotune_and_host_call(data):
     for k in range(len(PASSES)):
         c, ch, mx, ms = batch.tuning(k)
         assert 0 <= c <= min(mx, 4) and ch in (1, 2, 4, 8) and ms > 0
+    assert batch.lanes() in (1, 2)
     upload(batch, frames[0])
     batch.run(use_graph=True)
     batch.run(use_graph=True)
@@ -118,7 +126,7 @@ def test_autotune_and_host_call(data):
     for j in (1, 0):
         n0 = og.kernel_launch_count()
         outs = batch.process(frames[j])
-        assert og.kernel_launch_count() - n0 == 2 * len(PASSES)
+        assert og.kernel_launch_count() - n0 == 2 * batch.lanes() * len(PASSES)
         for i, (vec, pk) in enumerate(outs):
             assert np.array_equal(vec, expect[j][i][last][0]), f"process {j}: pair {i} vectors differ"
             assert np.array_equal(pk, expect[j][i][last][1]), f"process {j}: pair {i} peaks differ"
@@ -128,6 +136,8 @@ def test_autotune_and_host_call(data):
         batch.set_tuning(len(PASSES), 1, 1)
     with pytest.raises(og.OpivError):
         batch.set_schedule(7)
+    with pytest.raises(og.OpivError):
+        batch.set_lanes(0)
     batch.close()
 
 
@@ -150,6 +160,7 @@ def test_queue_groups_of_many_pairs():
     batch.run(use_graph=False)
     ref = [[batch.results(i, k) for k in range(len(passes))] for i in range(n)]
     batch.set_schedule(og.BATCH_QUEUE)
+    batch.set_lanes(1)                    # one lane: groups of 64 and 6 pairs
     n0 = og.kernel_launch_count()
     batch.run(use_graph=False)
     assert og.kernel_launch_count() - n0 == 2 * 2 * len(passes)
