@@ -13,7 +13,9 @@
 // derivatives of the fit, and either accumulates the vector-Jacobian
 // product of per-window cotangents (gu, gv) into image gradients, or the
 // propagated standard deviation of u and v for independent pixel noise.
-// One warp per window; lanes take the window's rows.
+// One warp per window; lanes take the window's columns and walk its rows,
+// so every load (and every gradient update) of a warp touches one row
+// segment of the frame (coalesced) rather than 32 rows.
 #include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -58,10 +60,10 @@ piv_adjoint_kernel(const PivParams p, int W, const int32_t* __restrict__ peaks,
     const int lx[5] = { px - W / 2, px - 1 - W / 2, px + 1 - W / 2, px - W / 2, px - W / 2 };
     const int ly[5] = { py - W / 2, py - W / 2, py - W / 2, py - 1 - W / 2, py + 1 - W / 2 };
 
-    // the five plane values: rows of the window split over the lanes
+    // the five plane values: columns of the window split over the lanes
     float R[5] = { 0.f, 0.f, 0.f, 0.f, 0.f };
-    for (int y = lane; y < W; y += 32)
-        for (int x = 0; x < W; ++x) {
+    for (int x = lane; x < W; x += 32)
+        for (int y = 0; y < W; ++y) {
             const float av = pix(fa, pitch, bx + x, by + y);
 #pragma unroll
             for (int v = 0; v < 5; ++v)
@@ -100,8 +102,8 @@ piv_adjoint_kernel(const PivParams p, int W, const int32_t* __restrict__ peaks,
 
     // per pixel: du/da[p] = sum_v gx[v] b[p + lag_v], du/db[q] = sum_v gx[v] a[q - lag_v]
     float su = 0.f, sv = 0.f;
-    for (int y = lane; y < W; y += 32)
-        for (int x = 0; x < W; ++x) {
+    for (int x = lane; x < W; x += 32)
+        for (int y = 0; y < W; ++y) {
             float dua = 0.f, dva = 0.f, dub = 0.f, dvb = 0.f;
 #pragma unroll
             for (int v = 0; v < 5; ++v) {
