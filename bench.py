@@ -230,10 +230,15 @@ def run_ours(args):
     frames = [(torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)) for _ in range(L2_ROTATION)]
     pitch = IMG * 2
 
+    tiles = {}
+
     def make_plan(precision):
         plan = og.Plan(IMG, IMG, np.uint16, IA, STEP, mode=og.CORR_COMPLEX, device=dev)
         assert plan.n == N_WIN
         plan.set_precision(precision)
+        # tensor-core plans: the autotuner times both tile shapes on the pair
+        fa, fb = frames[0]
+        tiles[precision] = plan.autotune(fa.data_ptr(), fb.data_ptr(), pitch, stream.cuda_stream)
         plan.set_timing(True)
         return plan
 
@@ -361,6 +366,9 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "windows_per_step": N_WIN, "ia": IA, "step": STEP,
                    "mode": "complex (FFT::cross_correlate)", "parallelism": f"replicas x{world}",
                    "path": "tensor-core DFT-GEMM, split BF16 (hi*hi + hi*lo + lo*hi), FP32 accumulate",
+                   "tile": {og.TILE_VERTICAL: "4 windows stacked in a grid column",
+                            og.TILE_HORIZONTAL: "4 windows side by side in a grid row"}.get(
+                                tiles.get(og.PREC_TC_SPLIT_BF16), "n/a") + " (autotuned)",
                    "streams": "steps alternate between two plans on two streams",
                    "l2": f"{L2_ROTATION} resident copies of the pair rotated per step "
                          f"({L2_ROTATION * 2 * IMG * IMG * 2 / 1e6:.0f} MB > 129 MB L2)"},

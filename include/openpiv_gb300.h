@@ -181,6 +181,21 @@ int opiv_plan_set_precision(opiv_plan* plan, int precision);
 int opiv_plan_create_tc(opiv_plan** plan, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
                         uint32_t dx, uint32_t dy, int mode, int limit_search, int precision,
                         int device);
+/* Tile shape of the 32 px tensor-core kernel (no reference counterpart):
+ * a CTA takes four windows stacked in a grid column (OPIV_TILE_VERTICAL:
+ * the 56 image rows of the four are transformed once; row steps of at most
+ * 8 px) or side by side in a grid row (OPIV_TILE_HORIZONTAL); AUTO stacks
+ * them where the step allows.  opiv_plan_get_tile returns the shape a pass
+ * of the plan uses (AUTO for plans without a choice: FFT path, 16/48/64 px).
+ * opiv_plan_autotune times both shapes on the given device frames (fastest
+ * of three passes after a warm-up, CUDA events on `stream`, outputs into the
+ * plan's own buffers) and keeps the faster; synchronous; a no-op for plans
+ * without a choice. */
+enum { OPIV_TILE_AUTO = 0, OPIV_TILE_VERTICAL = 1, OPIV_TILE_HORIZONTAL = 2 };
+int opiv_plan_set_tile(opiv_plan* plan, int tile);
+int opiv_plan_get_tile(const opiv_plan* plan);
+int opiv_plan_autotune(opiv_plan* plan, const void* d_frame_a, const void* d_frame_b,
+                       size_t pitch_bytes, void* stream);
 /* OPIV_OK, or OPIV_ERR_TIMEOUT if a tensor-core pass of this plan gave up
  * waiting for its MMAs since the last call (waits for the plan's work). */
 int opiv_plan_status(opiv_plan* plan);

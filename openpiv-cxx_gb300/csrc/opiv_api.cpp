@@ -157,6 +157,7 @@ struct opiv_plan {
     cudaEvent_t ev[3] = { nullptr, nullptr, nullptr };   // fp32 start, fp32 end, exact end
     int32_t* d_disp = nullptr;          // integer displacements (multi-pass plans)
     int precision = OPIV_PREC_FP32;
+    int tc_tile = OPIV_TILE_AUTO;       // 32 px tensor-core tile shape
     void* d_tc = nullptr;               // tensor-core constant matrices
     int* d_status = nullptr;            // tensor-core wait status
     float* d_planes = nullptr;          // optional plane output (tensor-core precisions)
@@ -297,6 +298,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.status = p->d_status;
         k.planes = p->d_planes;
         k.peds = p->d_peds;
+        k.tc_tile = p->tc_tile;
         if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
         CUDA_TRY(launch_piv_tc(k, (int)p->ia, p->dtype, p->mode, p->limit,
                                p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_SPLIT_FP16,
@@ -1528,6 +1530,81 @@ int opiv_batch_results(opiv_batch* b, int pair, int pass, opiv_vector* out_vec, 
 {
     if (!b || pair < 0 || pair >= (int)b->pairs.size()) return fail(OPIV_ERR_ARG, "no such pair");
     return opiv_multipass_results(b->pairs[pair], pass, out_vec, out_peak, out_disp);
+}
+
+namespace {
+// whether the plan's tensor-core kernel has a choice of tile shape
+bool tile_choice(const opiv_plan* p)
+{
+    return is_tc(p->precision) && p->ia == 32 && p->dy <= 8;
+}
+}  // namespace
+
+int opiv_plan_set_tile(opiv_plan* plan, int tile)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    if (tile != OPIV_TILE_AUTO && tile != OPIV_TILE_VERTICAL && tile != OPIV_TILE_HORIZONTAL)
+        return fail(OPIV_ERR_ARG, "unknown tile shape %d", tile);
+    plan->tc_tile = tile;
+    return OPIV_OK;
+}
+
+int opiv_plan_get_tile(const opiv_plan* plan)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    if (!is_tc(plan->precision) || plan->ia != 32) return OPIV_TILE_AUTO;
+    return (tile_choice(plan) && plan->tc_tile != OPIV_TILE_HORIZONTAL) ? OPIV_TILE_VERTICAL
+                                                                        : OPIV_TILE_HORIZONTAL;
+}
+
+int opiv_plan_autotune(opiv_plan* plan, const void* d_fa, const void* d_fb, size_t pitch_bytes, void* stream)
+{
+    if (!plan || !d_fa || !d_fb) return fail(OPIV_ERR_ARG, "null argument");
+    if (!tile_choice(plan)) return OPIV_OK;   // one shape only
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(plan->device);
+    auto done = [&](int st) { cudaSetDevice(prev); return st; };
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CUDA_TRY_D(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return done(fail(OPIV_ERR_CUDA, "cudaEventCreate"));
+    }
+    const bool timing = plan->timing;
+    plan->timing = false;
+    int rc = OPIV_OK, best = OPIV_TILE_VERTICAL;
+    float best_ms = 3.4e38f;
+    for (int tile : { OPIV_TILE_VERTICAL, OPIV_TILE_HORIZONTAL }) {
+        plan->tc_tile = tile;
+        float t_min = 3.4e38f;
+        for (int r = 0; r < 4 && rc == OPIV_OK; ++r) {   // one warm-up, three timed
+            cudaEventRecord(e0, s);
+            rc = run_pass(plan, d_fa, d_fb, pitch_bytes, plan->d_vec, plan->d_peak, s);
+            cudaEventRecord(e1, s);
+            if (rc != OPIV_OK) break;
+            const cudaError_t e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "autotune run");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0 && ms < t_min) t_min = ms;
+        }
+        if (rc != OPIV_OK) break;
+        if (t_min < best_ms) {
+            best_ms = t_min;
+            best = tile;
+        }
+    }
+    plan->timing = timing;
+    plan->tc_tile = best;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == OPIV_OK && plan->d_status) rc = opiv_plan_status(plan);
+    return done(rc);
 }
 
 int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_t pitch_bytes,

@@ -18,6 +18,10 @@ struct PivParams {
     int img_w = 0, img_h = 0;
     // regular grid: window k at (gx0 + (k % gnx) * gdx, gy0 + (k / gnx) * gdy)
     int gx0 = 0, gy0 = 0, gdx = 0, gdy = 0, gnx = 1;
+    // 32 px tensor-core kernel: tiles of four windows stacked in a grid
+    // column (1, rows transformed once; row steps <= 8 only) or side by side
+    // in a grid row (2); 0: stacked where allowed
+    int tc_tile = 0;
     const int32_t* win_xy = nullptr;   // explicit (x, y) list overrides the grid
     int64_t n_win = 0;
     opiv_vector* out_vec = nullptr;
@@ -118,6 +122,7 @@ struct PivQueue {
     const int32_t* flag_list = nullptr;
 };
 static_assert(kQueueMaxItems <= 256, "task_item holds pair numbers in one byte");
+static_assert(sizeof(PivParams) == 208, "descriptor size (queue parameter space)");
 static_assert(sizeof(PivParams) % 16 == 0, "descriptors are copied in 16-byte words");
 // tasks of a pair of n_win windows in the queue of window size w
 inline int fp32_queue_tasks(int w, int64_t n_win)

@@ -822,7 +822,8 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
 template <bool F16, bool SPLIT, int MODE, bool LIMIT>
 cudaError_t by_dtype(const PivParams& p, int dtype, const void* consts, cudaStream_t s)
 {
-    const bool vt = p.gdy > 0 && p.gdy <= 8;   // four stacked windows span <= 56 rows
+    // four stacked windows span <= 56 rows; the plan may ask for row tiles
+    const bool vt = p.tc_tile != 2 && p.gdy > 0 && p.gdy <= 8;
     if (dtype == kU8)
         return vt ? launch_t<F16, SPLIT, MODE, LIMIT, uint8_t, true>(p, consts, s)
                   : launch_t<F16, SPLIT, MODE, LIMIT, uint8_t, false>(p, consts, s);

@@ -58,7 +58,9 @@ SYMBOLS = [
     "opiv_process_pairs", "opiv_plan_adjoint", "opiv_batch_process", "opiv_plan_create_tc",
     "opiv_batch_set_schedule", "opiv_batch_set_tuning", "opiv_batch_get_tuning",
     "opiv_batch_autotune", "opiv_batch_set_lanes", "opiv_batch_get_lanes",
+    "opiv_plan_set_tile", "opiv_plan_get_tile", "opiv_plan_autotune",
 ]
+TILE_AUTO, TILE_VERTICAL, TILE_HORIZONTAL = 0, 1, 2
 BATCH_STREAMS, BATCH_QUEUE = 0, 1
 
 VECTOR_DTYPE = np.dtype([("x", np.float32), ("y", np.float32), ("u", np.float32),
@@ -115,6 +117,9 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_plan_exact_count.argtypes = [C.c_void_p]
     L.opiv_plan_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.opiv_plan_set_precision.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_set_tile.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_get_tile.argtypes = [C.c_void_p]
+    L.opiv_plan_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
     L.opiv_plan_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_float,
                                     C.c_float, C.c_void_p, C.c_void_p]
@@ -306,6 +311,18 @@ class Plan:
         _check(load().opiv_plan_adjoint(self._h, d_a, d_b, pitch, d_peak, d_cot or None,
                                         d_grad_a or None, d_grad_b or None, grad_pitch, var_a, var_b,
                                         d_sigma or None, stream or None))
+
+    def set_tile(self, tile: int):
+        """32 px tensor-core tile shape: TILE_AUTO, TILE_VERTICAL or TILE_HORIZONTAL."""
+        _check(load().opiv_plan_set_tile(self._h, tile))
+
+    def tile(self) -> int:
+        return _check(load().opiv_plan_get_tile(self._h))
+
+    def autotune(self, d_a: int, d_b: int, pitch: int, stream: int = 0) -> int:
+        """Times the tile shapes on device frames, keeps the faster; returns it."""
+        _check(load().opiv_plan_autotune(self._h, d_a, d_b, pitch, stream or None))
+        return self.tile()
 
     def set_precision(self, precision: int):
         """PREC_FP32 (default, reference-exact peaks), PREC_TC_SPLIT_BF16,

@@ -126,8 +126,8 @@ def test_host_find_peaks_and_fit(lib, orc):
 
 
 def test_batch_schedule_calls_check_arguments(lib):
-    """The queue-schedule calls of a batch reject a null batch before they
-    touch a device."""
+    """The queue-schedule calls of a batch and the tile calls of a plan
+    reject a null handle before they touch a device."""
     L = og.load()
     a, b, m = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
     assert L.opiv_batch_set_schedule(None, og.BATCH_QUEUE) == og.ERR_ARG
@@ -136,4 +136,7 @@ def test_batch_schedule_calls_check_arguments(lib):
     assert L.opiv_batch_autotune(None, None) == og.ERR_ARG
     assert L.opiv_batch_set_lanes(None, 2) == og.ERR_ARG
     assert L.opiv_batch_get_lanes(None) == og.ERR_ARG
+    assert L.opiv_plan_set_tile(None, og.TILE_VERTICAL) == og.ERR_ARG
+    assert L.opiv_plan_get_tile(None) == og.ERR_ARG
+    assert L.opiv_plan_autotune(None, None, None, 0, None) == og.ERR_ARG
     assert "null" in L.opiv_last_error().decode()

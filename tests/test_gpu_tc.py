@@ -245,3 +245,37 @@ def test_generic_limited_search_and_errors():
     with pytest.raises(og.OpivError) as e:
         og.Plan(256, 256, np.uint16, 48, 8, tensor_core=og.PREC_FP32)
     assert e.value.status == og.ERR_ARG
+
+
+def test_tile_shapes_and_autotune():
+    """Both tile shapes of the 32 px kernel (four windows stacked in a grid
+    column, four side by side in a grid row) meet the split-BF16 bounds
+    against the FP64 pass; the autotuner keeps one of them and a pass after
+    it equals a pass with that shape set explicitly."""
+    torch = _torch()
+    a, b = synth.config2(size=1024)
+    ref = run(a, b, 8, og.PREC_FP64)
+    h, w = a.shape
+    plan = og.Plan(w, h, a.dtype, W, 8)
+    assert plan.tile() == og.TILE_AUTO            # FFT path: no choice
+    plan.set_precision(og.PREC_TC_SPLIT_BF16)
+    assert plan.tile() == og.TILE_VERTICAL        # row step 8: stacked by default
+    outs = {}
+    for tile in (og.TILE_VERTICAL, og.TILE_HORIZONTAL):
+        plan.set_tile(tile)
+        assert plan.tile() == tile
+        vec, pk = plan.process(a, b)
+        plan.status()
+        got = {"vec": vec, "peak": np.where(pk >= 0, pk & og.PEAK_MASK, pk)}
+        rms, mx, mm = displacement_error(got, ref)
+        assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH, (tile, rms, mx, mm)
+        outs[tile] = (vec, pk)
+    da = torch.from_numpy(a.view(np.int16)).cuda()
+    db = torch.from_numpy(b.view(np.int16)).cuda()
+    chosen = plan.autotune(da.data_ptr(), db.data_ptr(), w * 2)
+    assert chosen in (og.TILE_VERTICAL, og.TILE_HORIZONTAL)
+    vec, pk = plan.process(a, b)
+    assert np.array_equal(vec, outs[chosen][0]) and np.array_equal(pk, outs[chosen][1])
+    with pytest.raises(og.OpivError):
+        plan.set_tile(3)
+    plan.close()
