@@ -64,6 +64,10 @@ FLOP_PER_WINDOW = 2 * 5 * IA * IA * math.log2(IA * IA) + 8 * IA * IA   # 110,592
 METRIC = "vectors/s"
 WORKLOAD = f"piv_pair_{IMG}x{IMG}_u16_ia{IA}_step{STEP}"
 L2_ROTATION = 4
+# DRAM bytes (read + write) of one launch of the timed kernels on this
+# workload, from ncu captures (the bench cannot profile itself)
+TC_TRAFFIC_BYTES = 69_884_160 + 3_193_344
+FP32_TRAFFIC_BYTES = 67_200_000 + 3_700_000
 
 
 def peaks_file():
@@ -377,7 +381,10 @@ def run_ours(args):
                 "call": "opiv_process_pairs (pinned host frames, copies overlapped with the passes)"},
         "gpu_launches": tc_launches,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                     "frac": achieved / bf16_peak, "traffic": None,
+                     "frac": achieved / bf16_peak, "traffic": TC_TRAFFIC_BYTES,
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                       "ncu capture of this workload (profiles/piv_tc_kernel_4096sq_u16_w32.md); "
+                                       f"algorithmic bytes {2 * IMG * IMG * 2 + N_WIN * 24}",
                      "kernel": "piv_tc_kernel<split,COMPLEX,u16>", "kernel_ms": statistics.mean(tc_ms),
                      "flop": "executed MMA FLOPs: 3 passes x (2 128x32 + 4 128x64 + 4 64x64 + 2 128x32 products, K=16) per 4 windows",
                      "peak_source": "bf16_tflops of MEASURED_PEAKS.json (cuBLAS burst, of measured)",
@@ -392,6 +399,9 @@ def run_ours(args):
             "roofline": {"bound": "fp32", "achieved": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12,
                          "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12 / fp32_peak,
+                         "traffic": FP32_TRAFFIC_BYTES,
+                         "traffic_source": "ncu capture of this workload "
+                                           "(profiles/piv_fp32_kernel_4096sq_u16_w32.md)",
                          "kernel": "piv_fp32_kernel<32,COMPLEX,u16>", "kernel_ms": statistics.mean(fp_ms),
                          "exact_pass_ms": statistics.mean(ex_ms),
                          "flop": "algorithmic: 2 x 5 N log2 N + 8 N, N = 1024, per window",
