@@ -169,3 +169,36 @@ def test_queue_groups_of_many_pairs():
             for g, r in zip(batch.results(i, k), ref[i][k]):
                 assert np.array_equal(g, r), f"pair {i} pass {k} differs"
     batch.close()
+
+
+@pytest.mark.parametrize("mode,limit,dtype", [(og.CORR_REAL, True, np.uint8),
+                                              (og.CORR_COMPLEX, True, np.float32),
+                                              (og.CORR_POCKET_REAL, False, np.uint8)])
+def test_queue_other_modes_and_pixel_types(mode, limit, dtype):
+    """REAL and pocket modes, limited peak search, 8-bit and float frames:
+    the queue schedule's windows equal the streams schedule's."""
+    sizes = [(384, 256), (512, 512), (264, 200)]
+    passes = [(64, 32), (32, 16), (16, 8)]
+    batch = og.Batch(sizes, dtype, passes, mode=mode, limit_search=limit)
+    for i, (w, h) in enumerate(sizes):
+        if dtype == np.uint8:
+            a, b = synth.particle_pair(h, w, ppp=0.02, i0_range=(150, 255), noise=3.0,
+                                       displacement=synth.lamb_oseen(w / 2.0, h / 2.0, offset=(0.7, -1.2)),
+                                       dtype=np.uint8, seed=synth.SEED_BASE + 4500 + i, full_scale=255.0)
+        else:
+            a, b = synth.particle_pair(h, w, ppp=0.02, i0_range=(0.6, 1.0), noise=0.02,
+                                       displacement=synth.lamb_oseen(w / 2.0, h / 2.0, offset=(0.7, -1.2)),
+                                       dtype=np.float32, seed=synth.SEED_BASE + 4600 + i, full_scale=None)
+        batch.upload(i, a, b)
+    batch.run(use_graph=False)
+    ref = [[batch.results(i, k) for k in range(len(passes))] for i in range(len(sizes))]
+    batch.set_schedule(og.BATCH_QUEUE)
+    for tuning in ((0, 1), (2, 2)):
+        for k in range(len(passes)):
+            batch.set_tuning(k, *tuning)
+        batch.run(use_graph=False)
+        for i in range(len(sizes)):
+            for k in range(len(passes)):
+                for g, r, name in zip(batch.results(i, k), ref[i][k], ("vectors", "peaks", "displacements")):
+                    assert np.array_equal(g, r, equal_nan=True), f"{tuning}: pair {i} pass {k} {name} differ"
+    batch.close()
