@@ -196,6 +196,14 @@ int opiv_plan_set_tile(opiv_plan* plan, int tile);
 int opiv_plan_get_tile(const opiv_plan* plan);
 int opiv_plan_autotune(opiv_plan* plan, const void* d_frame_a, const void* d_frame_b,
                        size_t pitch_bytes, void* stream);
+/* Test of the failure path (no counterpart in the reference).  With on = 1
+ * the 32 px tensor-core kernel of this plan issues no MMAs, so every CTA's
+ * first wait for them runs out after its bounded poll limit (about a
+ * second), the CTA stops, frees its tensor memory and flags the plan's
+ * status: the pass returns OPIV_ERR_TIMEOUT (its outputs are not valid) and
+ * the device stays usable.  on = 0 restores normal passes.
+ * OPIV_ERR_UNSUPPORTED for other plans. */
+int opiv_plan_test_mma_timeout(opiv_plan* plan, int on);
 /* OPIV_OK, or OPIV_ERR_TIMEOUT if a tensor-core pass of this plan gave up
  * waiting for its MMAs since the last call (waits for the plan's work). */
 int opiv_plan_status(opiv_plan* plan);

@@ -158,6 +158,7 @@ struct opiv_plan {
     int32_t* d_disp = nullptr;          // integer displacements (multi-pass plans)
     int precision = OPIV_PREC_FP32;
     int tc_tile = OPIV_TILE_AUTO;       // 32 px tensor-core tile shape
+    int mma_skip = 0;                   // failure-path test: no MMAs issued
     void* d_tc = nullptr;               // tensor-core constant matrices
     int* d_status = nullptr;            // tensor-core wait status
     float* d_planes = nullptr;          // optional plane output (tensor-core precisions)
@@ -299,6 +300,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.planes = p->d_planes;
         k.peds = p->d_peds;
         k.tc_tile = p->tc_tile;
+        k.mma_skip = p->mma_skip;
         if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
         CUDA_TRY(launch_piv_tc(k, (int)p->ia, p->dtype, p->mode, p->limit,
                                p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_SPLIT_FP16,
@@ -1539,6 +1541,15 @@ bool tile_choice(const opiv_plan* p)
     return is_tc(p->precision) && p->ia == 32 && p->dy <= 8;
 }
 }  // namespace
+
+int opiv_plan_test_mma_timeout(opiv_plan* plan, int on)
+{
+    if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
+    if (!is_tc(plan->precision) || plan->ia != 32)
+        return fail(OPIV_ERR_UNSUPPORTED, "the MMA-timeout test needs a 32 px tensor-core plan");
+    plan->mma_skip = on ? 1 : 0;
+    return OPIV_OK;
+}
 
 int opiv_plan_set_tile(opiv_plan* plan, int tile)
 {

@@ -44,6 +44,9 @@ struct PivParams {
     // previous window nearest to this window's centre.  Null: no offset.
     const int32_t* prev_disp = nullptr;
     int pgx0 = 0, pgy0 = 0, pgdx = 1, pgdy = 1, pgnx = 1, pgny = 1, pw = 0;
+    // test of the failure path: the 32 px tensor-core kernel issues no MMAs,
+    // so its bounded waits run out and it reports through `status`
+    int mma_skip = 0;
     int32_t* out_disp = nullptr;       // this pass's integer displacements (may be null)
     int* status = nullptr;             // tensor-core kernel: set to 1 if an MMA wait gave up
 };

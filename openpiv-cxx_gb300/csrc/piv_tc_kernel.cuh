@@ -301,7 +301,8 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 
     // wait for the committed MMAs; a wait that gives up aborts the CTA
     auto wait_mma = [&]() {
-        if (!tcx::mbar_wait(mbar, phase)) {
+        // after a wait has given up, the tile finishes without waiting again
+        if (!*abort_flag && !tcx::mbar_wait(mbar, phase)) {
             *abort_flag = 1;
             if (p.status) atomicExch(p.status, 1);
         }
@@ -389,7 +390,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 
         // ---- stage 1: H = X * G, one (VT) or two M-tiles of 128 rows, the
         // operand X in tensor memory
-        if (tid == 0) {
+        if (tid == 0 && !p.mma_skip) {
             tcx::fence_after();
             constexpr int NM = VT ? 1 : 2;
 #pragma unroll
@@ -495,7 +496,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 
         // ---- stage 2: conj of the column DFT: Re = U*C + V*(-S),
         // -Im = U*S + V*C
-        if (tid == 0) {   // N = 64: the U part against [C; S], the V part against [-S; C]
+        if (tid == 0 && !p.mma_skip) {   // N = 64: the U part against [C; S], the V part against [-S; C]
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
@@ -618,7 +619,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 
         // ---- stage 3: inverse column DFT, Re T = Pr*C + Pi*(-S),
         // Im T = Pr*S + Pi*C (M = 64)
-        if (tid == 0) {   // N = 64: the Pr part against [C; S], the Pi part against [-S; C]
+        if (tid == 0 && !p.mma_skip) {   // N = 64: the Pr part against [C; S], the Pi part against [-S; C]
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
@@ -652,7 +653,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         __syncthreads();
 
         // ---- stage 4: real inverse row DFT, D = T * C4
-        if (tid == 0) {
+        if (tid == 0 && !p.mma_skip) {
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 2; ++ks)

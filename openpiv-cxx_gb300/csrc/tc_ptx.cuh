@@ -82,19 +82,24 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Waits for the phase with the given parity to complete; gives up after a
-// bounded number of polls and returns false.
+// Waits for the phase with the given parity to complete; gives up after
+// kWaitCycles SM clock cycles (about a second at 2 GHz) and returns false.
+// The limit is on elapsed cycles, not on polls: a sleep between polls lasts
+// far longer than its nominal 32 ns, so a poll count gives no bound in time.
+constexpr long long kWaitCycles = 2000000000ll;
+
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity)
 {
     const uint32_t a = smem_addr(mbar);
-    for (int it = 0; it < (1 << 24); ++it) {
+    const long long t0 = clock64();
+    for (int it = 0;; ++it) {
         uint32_t done;
         asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
                      " selp.b32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(a), "r"(parity) : "memory");
         if (done) return true;
+        if (clock64() - t0 > kWaitCycles) return false;
         if (it > 64) __nanosleep(32);
     }
-    return false;
 }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols)

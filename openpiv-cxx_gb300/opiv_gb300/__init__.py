@@ -59,6 +59,7 @@ SYMBOLS = [
     "opiv_batch_set_schedule", "opiv_batch_set_tuning", "opiv_batch_get_tuning",
     "opiv_batch_autotune", "opiv_batch_set_lanes", "opiv_batch_get_lanes",
     "opiv_plan_set_tile", "opiv_plan_get_tile", "opiv_plan_autotune",
+    "opiv_plan_test_mma_timeout",
 ]
 TILE_AUTO, TILE_VERTICAL, TILE_HORIZONTAL = 0, 1, 2
 BATCH_STREAMS, BATCH_QUEUE = 0, 1
@@ -118,6 +119,7 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_plan_set_timing.argtypes = [C.c_void_p, C.c_int]
     L.opiv_plan_set_precision.argtypes = [C.c_void_p, C.c_int]
     L.opiv_plan_set_tile.argtypes = [C.c_void_p, C.c_int]
+    L.opiv_plan_test_mma_timeout.argtypes = [C.c_void_p, C.c_int]
     L.opiv_plan_get_tile.argtypes = [C.c_void_p]
     L.opiv_plan_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
     L.opiv_plan_adjoint.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
@@ -311,6 +313,11 @@ class Plan:
         _check(load().opiv_plan_adjoint(self._h, d_a, d_b, pitch, d_peak, d_cot or None,
                                         d_grad_a or None, d_grad_b or None, grad_pitch, var_a, var_b,
                                         d_sigma or None, stream or None))
+
+    def test_mma_timeout(self, on: bool):
+        """Failure-path test: the 32 px tensor-core kernel issues no MMAs, its
+        bounded waits run out and the pass raises ERR_TIMEOUT."""
+        _check(load().opiv_plan_test_mma_timeout(self._h, int(bool(on))))
 
     def set_tile(self, tile: int):
         """32 px tensor-core tile shape: TILE_AUTO, TILE_VERTICAL or TILE_HORIZONTAL."""

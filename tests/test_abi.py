@@ -139,4 +139,5 @@ def test_batch_schedule_calls_check_arguments(lib):
     assert L.opiv_plan_set_tile(None, og.TILE_VERTICAL) == og.ERR_ARG
     assert L.opiv_plan_get_tile(None) == og.ERR_ARG
     assert L.opiv_plan_autotune(None, None, None, 0, None) == og.ERR_ARG
+    assert L.opiv_plan_test_mma_timeout(None, 1) == og.ERR_ARG
     assert "null" in L.opiv_last_error().decode()

@@ -279,3 +279,28 @@ def test_tile_shapes_and_autotune():
     with pytest.raises(og.OpivError):
         plan.set_tile(3)
     plan.close()
+
+
+def test_mma_wait_timeout_reports_status():
+    """The failure path of the bounded MMA waits, without a GPU fault: with
+    no MMAs issued every CTA's wait runs out (about a second), the pass
+    raises ERR_TIMEOUT, and the next normal pass on the same plan and
+    context is correct."""
+    a, b = synth.config2(size=256)
+    h, w = a.shape
+    plan = og.Plan(w, h, a.dtype, W, 8)
+    plan.set_precision(og.PREC_TC_SPLIT_BF16)
+    good, good_pk = plan.process(a, b)
+    plan.test_mma_timeout(True)
+    with pytest.raises(og.OpivError) as e:
+        plan.process(a, b)
+    assert e.value.status == og.ERR_TIMEOUT
+    plan.test_mma_timeout(False)
+    vec, pk = plan.process(a, b)
+    assert np.array_equal(vec, good) and np.array_equal(pk, good_pk)
+    plan.close()
+    fft = og.Plan(w, h, a.dtype, W, 8)
+    with pytest.raises(og.OpivError) as e:
+        fft.test_mma_timeout(True)
+    assert e.value.status == og.ERR_UNSUPPORTED
+    fft.close()
