@@ -57,9 +57,13 @@ constexpr int kWarps = 4;   // warps per CTA
 // its sn below kSnTol * (1 + sn).  The parity tolerances are 1e-4 px and
 // 1e-5 * (1 + sn): sn = p0 / p1 is a ratio of plane values, and plane values
 // are specified to 1e-5 of the plane peak p0, which bounds the relative
-// error of p1 by 1e-5 * p0 / p1 = 1e-5 * sn.
-constexpr float kFitTol = 3e-5f;
-constexpr float kSnTol = 3e-6f;
+// error of p1 by 1e-5 * p0 / p1 = 1e-5 * sn.  The thresholds sit 1.6x inside
+// those tolerances (the rounding of the final FP32 logarithms, sums and
+// ratio adds ~1e-6 px and ~2e-7 relative on top of the bounds).  At 3e-5 /
+// 3e-6 three times as many 16 px windows went to the exact pass, nearly all
+// of them for the sn bound.
+constexpr float kFitTol = 6e-5f;
+constexpr float kSnTol = 6e-6f;
 #define kNegInf (-__int_as_float(0x7f800000))
 constexpr float kTwo23 = 8388608.0f;
 

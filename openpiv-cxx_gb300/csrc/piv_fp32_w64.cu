@@ -35,8 +35,9 @@ constexpr int N = W * W;
 constexpr int LD = W + 7;            // row stride (float2), odd: rows fall on distinct banks
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr float kFitTol = 3e-5f;
-constexpr float kSnTol = 3e-6f;
+// certification thresholds: as the 16 / 32 px kernel (piv_fp32.cuh)
+constexpr float kFitTol = 6e-5f;
+constexpr float kSnTol = 6e-6f;
 #define kNegInf64 (-__int_as_float(0x7f800000))
 
 // base-8 digit reversal of a 6-bit index (an involution)
