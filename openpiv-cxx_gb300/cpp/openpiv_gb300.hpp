@@ -10,6 +10,7 @@
 //   core::find_peaks (image_utils.impl.h:42-74)     find_peaks (peaks by value)
 //   core::fit_simple_gaussian (impl:77-101)         fit_simple_gaussian
 //   the loop of examples/process/main.cpp:189-302   piv_pass::process
+//   (no counterpart: multi-pass batches)           piv_batch
 //
 // Failures throw std::runtime_error whose message starts like the
 // reference's exception text (e.g. "dimensions must be power of 2").
@@ -229,8 +230,90 @@ public:
         return out;
     }
 
+    // OPIV_PREC_FP32 (reference-exact peaks), the tensor-core precisions
+    // (32 x 32 windows) or OPIV_PREC_FP64 (every window exact)
+    void set_precision(int precision) { check(opiv_plan_set_precision(plan_, precision)); }
+    // tile shape of the 32 px tensor-core kernel (OPIV_TILE_*), forced or
+    // timed on device frames by the autotuner; returns the shape in use
+    void set_tile(int tile) { check(opiv_plan_set_tile(plan_, tile)); }
+    int autotune(const void* d_frame_a, const void* d_frame_b, size_t pitch_bytes, void* stream = nullptr)
+    {
+        check(opiv_plan_autotune(plan_, d_frame_a, d_frame_b, pitch_bytes, stream));
+        return check_value(opiv_plan_get_tile(plan_));
+    }
+
 private:
+    static int check_value(int v)
+    {
+        check(v);
+        return v;
+    }
     opiv_plan* plan_ = nullptr;
+};
+
+// ---- batches ------------------------------------------------------------------
+// Many image pairs (sizes may differ) through one multi-pass schedule: pass
+// k >= 1 offsets each frame-B window by the previous pass's integer
+// displacement.  No counterpart in the reference (multi-pass is a TODO
+// there); see opiv_batch_* in the C ABI.  Schedules: OPIV_BATCH_STREAMS
+// (per-pair pass chains on fork streams) or OPIV_BATCH_QUEUE (per pass one
+// launch over a device work list of all pairs' windows); autotune() picks
+// the queue's launch shapes and lanes by timing them on the frames held.
+class piv_batch {
+public:
+    struct pass {
+        uint32_t ia = 0, step = 0;
+    };
+    piv_batch(const std::vector<size>& sizes, int dtype, const std::vector<pass>& passes, int mode,
+              bool limit_search = false, int device = 0)
+        : n_pairs_((int)sizes.size()), n_passes_((int)passes.size())
+    {
+        std::vector<uint32_t> w, h, ia, st;
+        for (const size& s : sizes) {
+            w.push_back(s.w);
+            h.push_back(s.h);
+        }
+        for (const pass& p : passes) {
+            ia.push_back(p.ia);
+            st.push_back(p.step);
+        }
+        check(opiv_batch_create(&batch_, n_pairs_, w.data(), h.data(), dtype, n_passes_, ia.data(),
+                                st.data(), mode, limit_search ? 1 : 0, device));
+    }
+    piv_batch(const piv_batch&) = delete;
+    piv_batch& operator=(const piv_batch&) = delete;
+    ~piv_batch() { opiv_batch_destroy(batch_); }
+
+    int pairs() const { return n_pairs_; }
+    int passes() const { return n_passes_; }
+    int64_t window_count(int pair, int pass_index) const
+    {
+        const int64_t n = opiv_batch_window_count(batch_, pair, pass_index);
+        check((int)(n < 0 ? n : 0));
+        return n;
+    }
+
+    template <typename T>
+    void upload(int pair, const image<T>& a, const image<T>& b, void* stream = nullptr)
+    {
+        check(opiv_batch_upload(batch_, pair, a.data(), b.data(), sizeof(T) * a.width(), stream));
+    }
+    void run(bool use_graph = true, void* stream = nullptr) { check(opiv_batch_run(batch_, use_graph ? 1 : 0, stream)); }
+    void set_schedule(int schedule) { check(opiv_batch_set_schedule(batch_, schedule)); }
+    void set_lanes(int lanes) { check(opiv_batch_set_lanes(batch_, lanes)); }
+    void autotune(void* stream = nullptr) { check(opiv_batch_autotune(batch_, stream)); }
+
+    // vectors of pair `pair`, pass `pass_index` (synchronises the device)
+    std::vector<opiv_vector> results(int pair, int pass_index) const
+    {
+        std::vector<opiv_vector> out((size_t)window_count(pair, pass_index));
+        check(opiv_batch_results(batch_, pair, pass_index, out.data(), nullptr, nullptr));
+        return out;
+    }
+
+private:
+    opiv_batch* batch_ = nullptr;
+    int n_pairs_ = 0, n_passes_ = 0;
 };
 
 // ---- image ingest ----------------------------------------------------------

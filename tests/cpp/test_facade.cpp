@@ -65,6 +65,11 @@ int main()
     EXPECT(q.size() == 1 && q[0].centre.x == 10 && q[0].centre.y == 8);
     const auto f = gb::fit_simple_gaussian(pl, q[0]);
     EXPECT(std::fabs(f.x - 10.3) < 1e-9 && std::fabs(f.y - 7.8) < 1e-9);
+
+    // batches and passes check their window sizes before touching a device
+    EXPECT(throws_with([] { gb::piv_batch b({ { 512, 512 } }, OPIV_U16, { { 24, 12 } }, OPIV_CORR_COMPLEX); },
+                       "power of 2"));
+    EXPECT(throws_with([] { gb::piv_pass p({ 512, 512 }, OPIV_U16, 24, 12, OPIV_CORR_COMPLEX); }, "power of 2"));
     std::printf("ok\n");
     return 0;
 }

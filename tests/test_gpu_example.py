@@ -42,3 +42,19 @@ def test_process_example_matches_oracle(orc, lib, tmp_path, ffttype, mode):
     # printed with 6 significant digits: |u| < 100 -> at most 5e-5 rounding
     assert np.nanmax(np.abs(np.where(nan, 0, got[:, 2:4] - ref[:, 2:4]))) < 1e-4
     assert "processing time" in r.stderr
+
+
+def test_cpp_facade_batch(lib, tmp_path):
+    """The C++ facade's piv_batch (tests/cpp/test_facade_batch.cpp): the
+    queue schedule after autotune() equals the streams schedule bit for bit
+    on two synthetic pairs through 64/32/16 px passes."""
+    exe = tmp_path / "test_facade_batch"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+                    "-I", os.path.join(ROOT, "openpiv-cxx_gb300", "cpp"),
+                    os.path.join(ROOT, "tests", "cpp", "test_facade_batch.cpp"),
+                    "-L", os.path.join(ROOT, "openpiv-cxx_gb300", "lib"), "-lopenpiv_gb300",
+                    "-Wl,-rpath," + os.path.join(ROOT, "openpiv-cxx_gb300", "lib"), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip() == "ok"
