@@ -559,7 +559,7 @@ def run_batch(args):
         # its vectors come back once its last pass ends
         batch.process_into(*ptrs)
 
-    e2e_steps = max(1, args.steps // 4)
+    e2e_steps = max(5, args.steps // 4)
 
     def e2e_time(schedule):
         batch.set_schedule(schedule)

@@ -503,8 +503,13 @@ __device__ __forceinline__ void fp32_task(const PivParams& p, const int task, fl
 
 extern __shared__ float2 fp32_dyn_smem[];
 
+// resident CTAs per SM the register budget is set for: a 16 px window's
+// transform needs half the registers of a 32 px one
+template <int W>
+constexpr int min_ctas() { return W == 16 ? 6 : 4; }
+
 template <int W, int MODE, bool LIMIT, typename PixT, bool PLANES, bool VEC>
-__global__ void __launch_bounds__(32 * kWarps, 4)
+__global__ void __launch_bounds__(32 * kWarps, min_ctas<W>())
 piv_fp32_kernel(const PivParams p)
 {
     fp32_task<W, MODE, LIMIT, PixT, PLANES, VEC>(p, (int)blockIdx.x * kWarps + (int)(threadIdx.x >> 5),
@@ -532,7 +537,7 @@ __device__ __forceinline__ const PivParams& warp_item(const PivQueue& q, int j, 
 // (thread 0 keeps the atomic's result in a register until the next
 // barrier), so no CTA stalls on the counter.  No CTA waits for another.
 template <int W, int MODE, bool LIMIT, typename PixT, bool VEC>
-__global__ void __launch_bounds__(32 * kWarps, 4)
+__global__ void __launch_bounds__(32 * kWarps, min_ctas<W>())
 piv_fp32_queue_kernel(const __grid_constant__ PivQueue q)
 {
     __shared__ unsigned int s_t0;
@@ -622,7 +627,7 @@ cudaError_t launch_w(const PivParams& p, int dtype, int mode, int limit, bool pl
 // The same work list dispatched by the hardware: CTA b runs tasks
 // kWarps * b ... (one per warp), no persistent loop.
 template <int W, int MODE, bool LIMIT, typename PixT, bool VEC>
-__global__ void __launch_bounds__(32 * kWarps, 4)
+__global__ void __launch_bounds__(32 * kWarps, min_ctas<W>())
 piv_fp32_list_kernel(const __grid_constant__ PivQueue q)
 {
     __shared__ __align__(16) unsigned char s_items[kWarps * sizeof(PivParams)];
