@@ -103,10 +103,13 @@ cudaError_t launch_piv_exact(const PivParams& p, int w, int dtype, int mode, int
 // window size), passed by value in the kernel's parameter space (read
 // through the constant cache): pair j is items[j]; its tasks are numbered
 // first_task[j] .. first_task[j + 1] - 1 and its windows first_win[j] ..
-// first_win[j + 1] - 1 in the queue's combined numbering.  A persistent
-// grid takes tasks from *head (zero before the launch); a task is what one
-// warp (16, 32 px: 2 * 32 / W windows) or one CTA (64 px: two windows) of
-// the single-pair kernel does.  Every item flags its uncertain windows into
+// first_win[j + 1] - 1 in the queue's combined numbering.  A task is what
+// one warp (16, 32 px: 2 * 32 / W windows) or one CTA (64 px: two windows)
+// of the single-pair kernel does.  Two launch shapes run the tasks: a
+// persistent grid whose CTAs take them from *head (zero before the launch),
+// or the list kernels, one CTA per task group handed out by the hardware
+// (the exact kernel reads items[]; the FP32 kernels copy items_g[task_item[t]]
+// into shared memory per task).  Every item flags its uncertain windows into
 // one list (flag_count / flag_list, combined window numbers), which the
 // exact queue kernel then re-decides for all the queue's pairs at once.
 constexpr int kQueueMaxItems = 64;
