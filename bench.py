@@ -246,19 +246,19 @@ def run_ours(args):
         plan.set_timing(True)
         return plan
 
-    def timed(precision, steps, warmup):
+    def timed(precision, steps, warmup, n_plans=2):
         """Device-resident passes over the pair, `steps` of them, alternating
         two plans on two streams (a pass's exact re-decision, a few SMs,
-        overlaps the next pass's main kernel): (seconds over all ranks,
-        main-kernel ms per step, exact-pass ms per step, launches, device
-        outputs of the last step)."""
-        plans = [make_plan(precision), make_plan(precision)]
-        streams = [stream, torch.cuda.Stream(device=dev)]
+        overlaps the next pass's main kernel), or one plan on one stream with
+        n_plans = 1: (seconds over all ranks, main-kernel ms per step,
+        exact-pass ms per step, launches, device outputs of the last step)."""
+        plans = [make_plan(precision) for _ in range(n_plans)]
+        streams = [stream, torch.cuda.Stream(device=dev)][:n_plans]
         outs = [(torch.empty((N_WIN, 5), dtype=torch.float32, device=dev),
                  torch.empty(N_WIN, dtype=torch.int32, device=dev)) for _ in plans]
 
         def step(k, i=None):
-            i = k & 1 if i is None else i
+            i = k % n_plans if i is None else i
             fa, fb = frames[k % L2_ROTATION]
             plans[i].process_device(fa.data_ptr(), fb.data_ptr(), pitch, outs[i][0].data_ptr(),
                                     outs[i][1].data_ptr(), streams[i].cuda_stream)
@@ -273,10 +273,10 @@ def run_ours(args):
         ev1 = torch.cuda.Event(enable_timing=True)
         ev_side = torch.cuda.Event()
         ev0.record(streams[0])
-        streams[1].wait_event(ev0)
+        streams[-1].wait_event(ev0)
         for k in range(steps):      # back to back: no host synchronisation inside
             step(k)
-        ev_side.record(streams[1])
+        ev_side.record(streams[-1])
         streams[0].wait_event(ev_side)
         ev1.record(streams[0])
         torch.cuda.synchronize()
@@ -285,7 +285,7 @@ def run_ours(args):
         launches = og.kernel_launch_count() - launches_before
         for p in plans:
             p.status()
-        last = (steps - 1) & 1
+        last = (steps - 1) % n_plans
         # kernel durations (the plan's events around its kernels) from a
         # separate loop on one plan that waits for each step
         main_ms, exact_ms = [], []
@@ -304,6 +304,11 @@ def run_ours(args):
     fp_el, fp_ms, ex_ms, fp_launches, fp_vec, fp_pk, fp_plan = timed(og.PREC_FP32, args.steps,
                                                                      args.warmup)
     exact_windows = fp_plan.exact_count()
+    # the same two paths with one plan on one stream (no overlap of
+    # neighbouring passes): a shorter run
+    n_single = max(3, args.steps // 2)
+    tc1_el = timed(og.PREC_TC_SPLIT_BF16, n_single, args.warmup, n_plans=1)[0]
+    fp1_el = timed(og.PREC_FP32, n_single, args.warmup, n_plans=1)[0]
 
     # ---- end to end through the host-buffer call (pinned host memory)
     ha = torch.from_numpy(a).pin_memory()
@@ -354,7 +359,8 @@ def run_ours(args):
         return
     peaks = peaks_file()
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12
     bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
     tc_s = statistics.mean(tc_ms) / 1e3
     fp_s = statistics.mean(fp_ms) / 1e3
@@ -373,9 +379,11 @@ def run_ours(args):
                    "tile": {og.TILE_VERTICAL: "4 windows stacked in a grid column",
                             og.TILE_HORIZONTAL: "4 windows side by side in a grid row"}.get(
                                 tiles.get(og.PREC_TC_SPLIT_BF16), "n/a") + " (autotuned)",
-                   "streams": "steps alternate between two plans on two streams",
+                   "streams": "steps alternate between two plans on two streams "
+                              "(one plan on one stream: single_stream_value)",
                    "l2": f"{L2_ROTATION} resident copies of the pair rotated per step "
                          f"({L2_ROTATION * 2 * IMG * IMG * 2 / 1e6:.0f} MB > 129 MB L2)"},
+        "single_stream_value": n_single * N_WIN * world / tc1_el,
         "e2e": {"value": tc_e2e, "unit": METRIC, "h2d_bytes_per_step": 2 * IMG * IMG * 2,
                 "d2h_bytes_per_step": N_WIN * (20 + 4),
                 "call": "opiv_process_pairs (pinned host frames, copies overlapped with the passes)"},
@@ -383,7 +391,7 @@ def run_ours(args):
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": achieved / bf16_peak, "traffic": TC_TRAFFIC_BYTES,
                      "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                                       "ncu capture of this workload (profiles/piv_tc_kernel_4096sq_u16_w32.md); "
+                                       "ncu capture of this workload; "
                                        f"algorithmic bytes {2 * IMG * IMG * 2 + N_WIN * 24}",
                      "kernel": "piv_tc_kernel<split,COMPLEX,u16>", "kernel_ms": statistics.mean(tc_ms),
                      "flop": "executed MMA FLOPs: 3 passes x (2 128x32 + 4 128x64 + 4 64x64 + 2 128x32 products, K=16) per 4 windows",
@@ -400,12 +408,13 @@ def run_ours(args):
                          "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12 / fp32_peak,
                          "traffic": FP32_TRAFFIC_BYTES,
-                         "traffic_source": "ncu capture of this workload "
-                                           "(profiles/piv_fp32_kernel_4096sq_u16_w32.md)",
+                         "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                           "launch, ncu capture of this workload",
                          "kernel": "piv_fp32_kernel<32,COMPLEX,u16>", "kernel_ms": statistics.mean(fp_ms),
                          "exact_pass_ms": statistics.mean(ex_ms),
                          "flop": "algorithmic: 2 x 5 N log2 N + 8 N, N = 1024, per window",
-                         "peak_source": f"152 SMs x 128 FP32 lanes x 2 x {sm_max:.0f} MHz"}},
+                         "peak_source": f"{n_sm} SMs x 128 FP32 lanes x 2 x {sm_max:.0f} MHz"},
+            "single_stream_value": n_single * N_WIN * world / fp1_el},
         "other_precisions": others,
         "clocks": clocks,
     }
@@ -582,7 +591,8 @@ def run_batch(args):
         return
     peaks = peaks_file()
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12
     achieved = flops * args.steps / graph / 1e12
     line = {
         "metric": "vectors/s (final pass)", "value": args.steps * final * world / graph,

@@ -356,11 +356,14 @@ int opiv_batch_autotune(opiv_batch* batch, void* stream);
  * (fixed-budget acquisition loops, hosts that own the device allocator): no
  * plan, no cudaMalloc / cudaFree.  Its scratch lives in one fixed device
  * array of about 4 MiB that every GPU using the library holds until exit.
- * Grids of more than 1,048,576 windows are rejected (OPIV_ERR_CAPACITY).
+ * Limits: 16 or 32 px windows only (64 px: OPIV_ERR_UNSUPPORTED); grids of
+ * more than 1,048,576 windows are rejected (OPIV_ERR_CAPACITY); the
+ * PocketFFT modes run the COMPLEX kernels, as opiv_plan_create does.
  * The first call on a device does a one-time set-up (address lookup and a
- * synchronous table upload): make it before any stream capture.  All calls
- * share the scratch; calls that overlap on the GPU race, so order them on
- * one stream.  Uses the current device; asynchronous on `stream`. */
+ * synchronous table upload): make it before any stream capture.  The set-up
+ * is not repeated, so the call is not usable after a cudaDeviceReset.  All
+ * calls share the scratch; calls that overlap on the GPU race, so order them
+ * on one stream.  Uses the current device; asynchronous on `stream`. */
 int opiv_process_pair_device_noalloc(const void* d_frame_a, const void* d_frame_b,
                                      size_t pitch_bytes, uint32_t img_w, uint32_t img_h, int dtype,
                                      uint32_t ia, uint32_t dx, uint32_t dy, int mode,
@@ -376,6 +379,27 @@ int opiv_process_pair_device_noalloc(const void* d_frame_a, const void* d_frame_
  * FFT::cross_correlate / cross_correlate_real: fft.h:188-227. */
 int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int64_t n, int mode,
                                int exact, double* out_planes, int device);
+
+/* ---- per-window spectra (FFT::transform, transform_real, auto_correlate) -- */
+/* algos::direction (fft_common.h:9-12) */
+enum { OPIV_FORWARD = 0, OPIV_REVERSE = 1 };
+/* n windows of w x w, row-major, complex values interleaved (re, im).
+ * All three run the exact double kernel (the reference's butterflies,
+ * twiddle tables and complex products, bit-identical results) on the GPU;
+ * host buffers, synchronous.  w: a power of 2 from 4 to 64.
+ * FFT::transform(input, d), fft.h:87-119: unnormalised 2-D transform of
+ *   `in` (2 n w^2 doubles) into `out`. */
+int opiv_transform_batch(const double* in, uint32_t w, int64_t n, int direction, double* out,
+                         int device);
+/* FFT::transform_real(a, b, d), fft.h:123-186: a, b real (n w^2 doubles
+ * each); out_a, out_b the two spectra of the two-for-one transform with the
+ * reference's partial unpack (rows [1, H/2) x columns [1, W) and their
+ * mirrors; row 0, row H/2 and column 0 zero). */
+int opiv_transform_real_batch(const double* a, const double* b, uint32_t w, int64_t n, int direction,
+                              double* out_a, double* out_b, int device);
+/* FFT::auto_correlate(a), fft.h:229-242: real(IFFT(|FFT(a)|^2)) after
+ * swap_quadrants, as a complex image with zero imaginary parts. */
+int opiv_auto_correlate_batch(const double* in, uint32_t w, int64_t n, double* out, int device);
 
 /* ---- image ingest and vector output (host) ------------------------------- */
 /* The reference's loaders (loaders/pnm_image_loader.cpp:199-226, PNM P5/P6,
@@ -396,6 +420,9 @@ int opiv_vectors_write(const char* path, const opiv_vector* vectors, int64_t n);
  * up to num_peaks centres (x, y) and values, highest first; returns count. */
 int opiv_find_peaks(const double* im, uint32_t w, uint32_t h, uint16_t num_peaks, uint32_t radius,
                     int32_t* out_xy, double* out_value);
+/* The two offsets fit_simple_gaussian adds to a 3x3 view's midpoint
+ * (image_utils.impl.h:86-98): v9 row-major, out_fxfy = (fx, fy). */
+int opiv_gaussian_offsets(const double* v9, double* out_fxfy);
 /* core::fit_simple_gaussian on the 3x3 around (px, py): image_utils.impl.h:77-101 */
 int opiv_fit_simple_gaussian(const double* plane, uint32_t w, uint32_t h, int32_t px, int32_t py,
                              double* out_xy);

@@ -24,6 +24,14 @@
 //   * At most kNoAllocMaxWindows windows per call (every grid of a 4096^2
 //     image down to 16 x 16 windows at step 4 fits); larger requests are
 //     rejected with OPIV_ERR_CAPACITY before anything runs.
+//   * 16 and 32 px windows only (the twiddle tables of the exact pass are
+//     sized for those two); 64 px windows are refused with
+//     OPIV_ERR_UNSUPPORTED.  All four correlation modes are taken; the
+//     PocketFFT modes run the COMPLEX kernels, as the plan path does.
+//   * The set-up is not repeated: after a cudaDeviceReset (or any teardown
+//     of the device's primary context) the cached address and the uploaded
+//     tables are stale, so the entry point must not be used again in that
+//     process.
 //   * The first call on a device performs the set-up (symbol address lookup
 //     and a synchronous upload of the twiddle tables).  Make that first call
 //     before any stream capture begins.
@@ -59,9 +67,8 @@ constexpr size_t kScratchBytes = kOffTw32 + sizeof(double2) * 2 * 32;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 // Same calibration as the plan-based path: error-bound factor of the FP32
-// kernel, and the number of CTAs of the exact pass.
+// kernel; the exact pass runs two CTAs per SM.
 constexpr float kNoAllocKappa = 8.0f;
-constexpr int kNoAllocExactBlocks = 152 * 2;
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
@@ -134,8 +141,11 @@ extern "C" int opiv_process_pair_device_noalloc(const void* d_frame_a, const voi
     if (!d_frame_a || !d_frame_b || !d_out_vec) return na_fail(OPIV_ERR_ARG, "null argument");
     const size_t px = pixel_bytes(dtype);
     if (px == 0) return na_fail(OPIV_ERR_ARG, "unknown pixel type %d", dtype);
-    if (mode != OPIV_CORR_REAL && mode != OPIV_CORR_COMPLEX)
+    if (mode != OPIV_CORR_REAL && mode != OPIV_CORR_COMPLEX && mode != OPIV_CORR_POCKET &&
+        mode != OPIV_CORR_POCKET_REAL)
         return na_fail(OPIV_ERR_ARG, "unknown correlation mode %d", mode);
+    // the PocketFFT modes are the true circular correlation: COMPLEX kernels
+    if (mode != OPIV_CORR_REAL) mode = OPIV_CORR_COMPLEX;
     // grid checks and geometry as generate_cartesian_grid (grid.impl.h:29-48)
     if ((uint64_t)img_w * img_h == 0) return na_fail(OPIV_ERR_IMAGE_EMPTY, "image size must be non-zero");
     if (ia == 0) return na_fail(OPIV_ERR_IA_EMPTY, "interrogation size must be non-zero");
@@ -191,7 +201,7 @@ extern "C" int opiv_process_pair_device_noalloc(const void* d_frame_a, const voi
     if ((e = launch_piv_fp32(k, (int)ia, dtype, mode, limit_search ? 1 : 0, false, s)) != cudaSuccess)
         return na_fail(OPIV_ERR_CUDA, "FP32 pass: %s", cudaGetErrorString(e));
     if ((e = launch_piv_exact(k, (int)ia, dtype, mode, limit_search ? 1 : 0, true,
-                              kNoAllocExactBlocks, s)) != cudaSuccess)
+                              2 * device_sm_count(device), s)) != cudaSuccess)
         return na_fail(OPIV_ERR_CUDA, "exact pass: %s", cudaGetErrorString(e));
     return OPIV_OK;
 }

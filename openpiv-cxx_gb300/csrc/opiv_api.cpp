@@ -7,6 +7,7 @@
 // start with the same text as the exceptions the reference throws.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -108,8 +109,10 @@ std::vector<double2> reference_twiddles(uint32_t n, int dir)
     return t;
 }
 
-constexpr int kExactBlocks = 152 * 2;   // CTAs of the exact pass (two per SM)
-constexpr int kExactAllBlocks = 152 * 8; // CTAs when every window takes the exact kernel
+// CTAs of the exact pass: two per SM for a flagged list, eight per SM when
+// every window takes the exact kernel
+int exact_blocks(int device) { return 2 * device_sm_count(device); }
+int exact_all_blocks(int device) { return 8 * device_sm_count(device); }
 
 bool is_tc(int precision)
 {
@@ -135,6 +138,17 @@ int opiv::record_error(int status, const char* message)
 {
     g_last_error = message;
     return status;
+}
+
+int opiv::device_sm_count(int device)
+{
+    static std::atomic<int> cache[64];
+    if (device < 0 || device >= 64) return 1;
+    int n = cache[device].load();
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0) return 1;
+    cache[device].store(n);
+    return n;
 }
 
 struct opiv_plan {
@@ -315,7 +329,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
     }
     if (p->precision == OPIV_PREC_FP64) {
         if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
-        CUDA_TRY(launch_piv_exact(k, (int)p->ia, p->dtype, p->mode, p->limit, false, kExactAllBlocks, s));
+        CUDA_TRY(launch_piv_exact(k, (int)p->ia, p->dtype, p->mode, p->limit, false, exact_all_blocks(p->device), s));
         ++g_launches;
         if (p->timing) {
             CUDA_TRY(cudaEventRecord(p->ev[1], s));
@@ -327,7 +341,7 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
     CUDA_TRY(launch_piv_fp32(k, (int)p->ia, p->dtype, p->mode, p->limit, false, s));
     ++g_launches;
     if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[1], s));
-    CUDA_TRY(launch_piv_exact(k, (int)p->ia, p->dtype, p->mode, p->limit, true, kExactBlocks, s));
+    CUDA_TRY(launch_piv_exact(k, (int)p->ia, p->dtype, p->mode, p->limit, true, exact_blocks(p->device), s));
     ++g_launches;
     if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[2], s));
     return OPIV_OK;
@@ -827,7 +841,7 @@ struct batch_queue_pass {
     int ia = 0, dtype = 0, mode = 0, limit = 0;
     bool vec = true;                    // every pair's A rows 16-byte aligned
     int max_ctas = 0;                   // resident CTAs per SM of the queue kernel
-    int exact_blocks = kExactBlocks;    // CTAs of the exact launch: every resident slot
+    int exact_blocks = 0;               // CTAs of the exact launch: every resident slot
     int ctas_per_sm = -1;               // tuning: -1 untuned (the resident limit), 0 hardware dispatch
     int chunk = 1;                      // tuning: tasks per dequeue
     float tuned_ms = 0.f;               // the autotuner's fastest pass time
@@ -1823,6 +1837,116 @@ int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int
     cudaFree(d_tw);
     cudaSetDevice(prev);
     return rc;
+}
+
+// FFT::transform / transform_real / auto_correlate on a batch of windows
+// (fft.h:87-186, :229-242): host buffers, the exact double kernel, one CTA
+// per window.  in_c / out_* are interleaved complex (re, im) doubles.
+static int spectral_batch(int op, const double* in_c, const double* in_ra, const double* in_rb,
+                          uint32_t w, int64_t n, int direction, double* out_a, double* out_b,
+                          int device, const char* name)
+{
+    if (n < 0) return fail(OPIV_ERR_ARG, "%s: negative window count", name);
+    if (direction != OPIV_FORWARD && direction != OPIV_REVERSE)
+        return fail(OPIV_ERR_ARG, "%s: unknown direction %d", name, direction);
+    if (!is_pow2(w)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", w, w);
+    if (!exact_supports((int)w)) return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", w, w);
+    if (n == 0) return OPIV_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) return fail(OPIV_ERR_NO_DEVICE, "cannot use device %d", device);
+    const size_t N = (size_t)w * w * n;
+    double2 *d_in = nullptr, *d_oa = nullptr, *d_ob = nullptr, *d_tw = nullptr;
+    double *d_ra = nullptr, *d_rb = nullptr;
+    int rc = OPIV_OK;
+    cudaError_t e = cudaSuccess;
+    do {
+        std::vector<double2> tw = reference_twiddles(w, direction == OPIV_REVERSE ? +1 : -1);
+        if (op == kSpectralAuto) {
+            const std::vector<double2> tr = reference_twiddles(w, +1);
+            tw = reference_twiddles(w, -1);
+            tw.insert(tw.end(), tr.begin(), tr.end());
+        }
+        if ((e = cudaMalloc(&d_tw, sizeof(double2) * tw.size())) != cudaSuccess) break;
+        if ((e = cudaMemcpy(d_tw, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice)) != cudaSuccess) break;
+        if ((e = cudaMalloc(&d_oa, sizeof(double2) * N)) != cudaSuccess) break;
+        SpectralParams q;
+        q.w = (int)w;
+        q.n = n;
+        q.tw = d_tw;
+        q.out_a = d_oa;
+        if (op == kSpectralReal) {
+            if ((e = cudaMalloc(&d_ob, sizeof(double2) * N)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&d_ra, sizeof(double) * N)) != cudaSuccess) break;
+            if ((e = cudaMalloc(&d_rb, sizeof(double) * N)) != cudaSuccess) break;
+            if ((e = cudaMemcpy(d_ra, in_ra, sizeof(double) * N, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+            if ((e = cudaMemcpy(d_rb, in_rb, sizeof(double) * N, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+            q.in_ra = d_ra;
+            q.in_rb = d_rb;
+            q.out_b = d_ob;
+        } else {
+            if ((e = cudaMalloc(&d_in, sizeof(double2) * N)) != cudaSuccess) break;
+            if ((e = cudaMemcpy(d_in, in_c, sizeof(double2) * N, cudaMemcpyHostToDevice)) != cudaSuccess) break;
+            q.in_c = d_in;
+        }
+        const int blocks = (int)std::min<int64_t>(n, 8 * (int64_t)device_sm_count(device));
+        if ((e = launch_spectral_exact(q, op, blocks, nullptr)) != cudaSuccess) break;
+        ++g_launches;
+        if ((e = cudaMemcpy(out_a, d_oa, sizeof(double2) * N, cudaMemcpyDeviceToHost)) != cudaSuccess) break;
+        if (op == kSpectralReal &&
+            (e = cudaMemcpy(out_b, d_ob, sizeof(double2) * N, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            break;
+        e = cudaDeviceSynchronize();
+    } while (0);
+    if (e != cudaSuccess) rc = cuda_fail(e, name);
+    cudaFree(d_in);
+    cudaFree(d_oa);
+    cudaFree(d_ob);
+    cudaFree(d_tw);
+    cudaFree(d_ra);
+    cudaFree(d_rb);
+    cudaSetDevice(prev);
+    return rc;
+}
+
+int opiv_transform_batch(const double* in, uint32_t w, int64_t n, int direction, double* out,
+                         int device)
+{
+    if (!in || !out) return fail(OPIV_ERR_ARG, "null argument");
+    return spectral_batch(kSpectralTransform, in, nullptr, nullptr, w, n, direction, out, nullptr, device,
+                          "opiv_transform_batch");
+}
+
+int opiv_transform_real_batch(const double* a, const double* b, uint32_t w, int64_t n, int direction,
+                              double* out_a, double* out_b, int device)
+{
+    if (!a || !b || !out_a || !out_b) return fail(OPIV_ERR_ARG, "null argument");
+    return spectral_batch(kSpectralReal, nullptr, a, b, w, n, direction, out_a, out_b, device,
+                          "opiv_transform_real_batch");
+}
+
+int opiv_auto_correlate_batch(const double* in, uint32_t w, int64_t n, double* out, int device)
+{
+    if (!in || !out) return fail(OPIV_ERR_ARG, "null argument");
+    return spectral_batch(kSpectralAuto, in, nullptr, nullptr, w, n, OPIV_FORWARD, out, nullptr, device,
+                          "opiv_auto_correlate_batch");
+}
+
+// The 3-point Gaussian offsets of fit_simple_gaussian (image_utils.impl.h:
+// 86-98) on a 3 x 3 block, row-major: the caller adds them to its view's
+// midpoint, as the reference does.
+int opiv_gaussian_offsets(const double* v9, double* out_fxfy)
+{
+    if (!v9 || !out_fxfy) return fail(OPIV_ERR_ARG, "null argument");
+    auto f = [](double l, double c, double r) {
+        const double num = std::log(l) - std::log(r);
+        const double den = 2.0 * (std::log(l) + std::log(r) - 2.0 * std::log(c));
+        if (den == 0.0) return 0.0;
+        return num / den;
+    };
+    out_fxfy[0] = f(v9[3], v9[4], v9[5]);
+    out_fxfy[1] = f(v9[1], v9[4], v9[7]);
+    return OPIV_OK;
 }
 
 // core::find_peaks, image_utils.impl.h:42-74 (host).  The sort is the

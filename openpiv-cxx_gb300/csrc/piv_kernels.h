@@ -99,6 +99,28 @@ bool exact_supports(int w);
 cudaError_t launch_piv_exact(const PivParams& p, int w, int dtype, int mode, int limit,
                              bool use_list, int blocks, cudaStream_t s);
 
+// The per-window spectral API (FFT::transform, transform_real,
+// auto_correlate; fft.h:87-186, :229-242) on n windows of w x w, in the
+// exact kernel's double arithmetic (piv_exact.cu).  All device pointers:
+//  kSpectralTransform  in_c (complex) -> out_a, with tw = the forward or
+//                      the reverse table;
+//  kSpectralReal       in_ra, in_rb (real) -> out_a, out_b (the partial
+//                      unpack), tw = one direction's table;
+//  kSpectralAuto       in_c -> out_a (real part, quadrant-swapped, zero
+//                      imaginary parts), tw = forward table then reverse.
+enum { kSpectralTransform = 0, kSpectralReal = 1, kSpectralAuto = 2 };
+struct SpectralParams {
+    int w = 0;
+    int64_t n = 0;
+    const double2* in_c = nullptr;
+    const double* in_ra = nullptr;
+    const double* in_rb = nullptr;
+    double2* out_a = nullptr;
+    double2* out_b = nullptr;
+    const double2* tw = nullptr;
+};
+cudaError_t launch_spectral_exact(const SpectralParams& q, int op, int blocks, cudaStream_t s);
+
 // Device work queue of one pass over up to kQueueMaxItems image pairs (one
 // window size), passed by value in the kernel's parameter space (read
 // through the constant cache): pair j is items[j]; its tasks are numbered
@@ -163,5 +185,9 @@ int exact_queue_max_ctas_per_sm(int w);
 // Records `message` as the calling thread's last error (opiv_last_error)
 // and returns `status`.
 int record_error(int status, const char* message);
+
+// Streaming multiprocessors of `device` (queried once per device, then
+// cached); 1 if the query fails, so that grid sizes stay positive.
+int device_sm_count(int device);
 
 }  // namespace opiv

@@ -84,21 +84,25 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count)
 
 // Waits for the phase with the given parity to complete; gives up after
 // kWaitCycles SM clock cycles (about a second at 2 GHz) and returns false.
-// The limit is on elapsed cycles, not on polls: a sleep between polls lasts
-// far longer than its nominal 32 ns, so a poll count gives no bound in time.
+// The limit is on elapsed cycles, not on polls.  Each try_wait carries a
+// suspend-time hint: the warp sleeps in the barrier unit until the phase
+// completes (or the hint, kSuspendNs, runs out) instead of re-issuing the
+// poll, which leaves the issue slots and the shared-memory pipe to the other
+// warps of the SM.
 constexpr long long kWaitCycles = 2000000000ll;
+constexpr uint32_t kSuspendNs = 1000000u;
 
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity)
 {
     const uint32_t a = smem_addr(mbar);
     const long long t0 = clock64();
-    for (int it = 0;; ++it) {
+    for (;;) {
         uint32_t done;
-        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                     " selp.b32 %0, 1, 0, p;\n}\n" : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+                     " selp.b32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done) : "r"(a), "r"(parity), "r"(kSuspendNs) : "memory");
         if (done) return true;
         if (clock64() - t0 > kWaitCycles) return false;
-        if (it > 64) __nanosleep(32);
     }
 }
 

@@ -7,6 +7,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "openpiv-cxx_gb300")
+# the reference sources (read-only), where this machine has them
+REFERENCE = os.environ.get("OPENPIV_REFERENCE", "/root/reference")
 for p in (PKG, ROOT):
     if p not in sys.path:
         sys.path.insert(0, p)
@@ -45,8 +47,9 @@ def ref_lib():
     from oracle import oracle
 
     if not oracle.available("ref"):
-        if os.path.isdir("/root/reference/openpiv"):
-            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+        if os.path.isdir(os.path.join(REFERENCE, "openpiv")):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REFERENCE}"],
+                           check=True)
         else:
             pytest.skip("reference sources not on this machine")
     return oracle.get("ref")

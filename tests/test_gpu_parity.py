@@ -241,6 +241,8 @@ def test_device_buffers_match_host_call():
     dvec = torch.zeros((plan.n, 5), dtype=torch.float32, device="cuda")
     dpk = torch.zeros(plan.n, dtype=torch.int32, device="cuda")
     s = torch.cuda.Stream()
+    # uploads and fills ran on torch's current stream: order the pass after them
+    s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
         plan.process_device(da.data_ptr(), db.data_ptr(), 1024, dvec.data_ptr(), dpk.data_ptr(),
                             s.cuda_stream)

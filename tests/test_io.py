@@ -8,7 +8,7 @@ import pytest
 
 import opiv_gb300 as og
 
-REF_DATA = "/root/reference/examples"
+REF_DATA = os.path.join(os.environ.get("OPENPIV_REFERENCE", "/root/reference"), "examples")
 
 
 def write_pnm(path, img, rgb=False):
