@@ -376,7 +376,99 @@ cudaError_t queue_t(const PivQueue& q, int w, int mode, int limit, int blocks, c
     return cudaGetLastError();
 }
 
+// ---- the per-window spectral API: FFT::transform, transform_real and
+// auto_correlate (fft.h:87-186, :229-242) on a batch of windows, in the
+// reference's double arithmetic (the same butterflies, twiddle tables,
+// complex products and unpack as the correlation above).  One CTA per
+// window (CTAs stride over the batch); X is one W x W double2 tile of
+// shared memory.
+template <int OP>
+__global__ void __launch_bounds__(kThreads)
+spectral_exact_kernel(const SpectralParams q)
+{
+    extern __shared__ double2 X[];
+    const int W = q.w, N = W * W, t = threadIdx.x;
+    for (int64_t w = blockIdx.x; w < q.n; w += gridDim.x) {
+        const size_t o = (size_t)w * N;
+        // transform: the input converted to complex (image::operator=,
+        // image.h:136-145); transform_real: join_from_channels(a, b)
+        // (image_utils.impl.h:288-315); auto_correlate: transform(a)
+        for (int i = t; i < N; i += blockDim.x)
+            X[i] = OP == kSpectralReal ? make_double2(q.in_ra[o + i], q.in_rb[o + i]) : q.in_c[o + i];
+        __syncthreads();
+        fft2d(X, W, q.tw);
+        if (OP == kSpectralTransform) {
+            for (int i = t; i < N; i += blockDim.x) q.out_a[o + i] = X[i];
+        } else if (OP == kSpectralReal) {
+            // the partial unpack of fft.h:163-183 into two zeroed spectra:
+            // rows [1, H/2) x columns [1, W) and their mirrors
+            for (int i = t; i < N; i += blockDim.x) {
+                q.out_a[o + i] = make_double2(0.0, 0.0);
+                q.out_b[o + i] = make_double2(0.0, 0.0);
+            }
+            __syncthreads();
+            const int npairs = (W / 2 - 1) * (W - 1);
+            for (int k = t; k < npairs; k += blockDim.x) {
+                const int h = 1 + k / (W - 1), x = 1 + k % (W - 1);
+                const int i = h * W + x, m = (W - h) * W + (W - x);
+                const double2 t1 = X[i], t2 = X[m];
+                const double2 half = make_double2(0.5, 0.0);
+                const double2 av = e_mul(half, e_add(t1, e_conj(t2)));
+                double2 bv = e_mul(half, e_sub(t1, e_conj(t2)));
+                bv = make_double2(bv.y, __dmul_rn(-1.0, bv.x));
+                q.out_a[o + i] = av;
+                q.out_a[o + m] = e_conj(av);
+                q.out_b[o + i] = bv;
+                q.out_b[o + m] = e_conj(bv);
+            }
+        } else {
+            // |A|^2 = (A * conj A).real (pixel_types.h:198), as a complex
+            // image with zero imaginary parts; the unnormalised inverse;
+            // its real part, quadrant-swapped (image_utils.impl.h:367-386)
+            for (int i = t; i < N; i += blockDim.x) X[i] = make_double2(e_mul(X[i], e_conj(X[i])).x, 0.0);
+            __syncthreads();
+            fft2d(X, W, q.tw + W);
+            for (int i = t; i < N; i += blockDim.x) {
+                const int y = i / W, x = i % W;
+                const int sy = (y + W / 2) % W, sx = (x + W / 2) % W;
+                q.out_a[o + i] = make_double2(X[sy * W + sx].x, 0.0);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int OP>
+cudaError_t spectral_t(const SpectralParams& q, int blocks, cudaStream_t s)
+{
+    const size_t smem = sizeof(double2) * (size_t)q.w * q.w;
+    static std::atomic<uint64_t> attr_done{ 0 };
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(attr_done.load() & bit)) {
+        const cudaError_t e = cudaFuncSetAttribute(spectral_exact_kernel<OP>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)(sizeof(double2) * kMaxW * kMaxW));
+        if (e != cudaSuccess) return e;
+        attr_done.fetch_or(bit);
+    }
+    spectral_exact_kernel<OP><<<blocks, kThreads, smem, s>>>(q);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_spectral_exact(const SpectralParams& q, int op, int blocks, cudaStream_t s)
+{
+    if (!exact_supports(q.w) || blocks <= 0 || q.n <= 0) return cudaErrorInvalidValue;
+    switch (op) {
+    case kSpectralTransform: return spectral_t<kSpectralTransform>(q, blocks, s);
+    case kSpectralReal: return spectral_t<kSpectralReal>(q, blocks, s);
+    case kSpectralAuto: return spectral_t<kSpectralAuto>(q, blocks, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 int exact_queue_max_ctas_per_sm(int w)
 {

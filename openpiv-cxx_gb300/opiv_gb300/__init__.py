@@ -49,6 +49,8 @@ SYMBOLS = [
     "opiv_process_pair_device", "opiv_plan_exact_count", "opiv_plan_set_timing",
     "opiv_plan_last_timing", "opiv_cross_correlate_batch",
     "opiv_find_peaks", "opiv_fit_simple_gaussian", "opiv_process_pair_device_noalloc",
+    "opiv_transform_batch", "opiv_transform_real_batch", "opiv_auto_correlate_batch",
+    "opiv_gaussian_offsets",
     "opiv_image_info", "opiv_image_load", "opiv_vectors_write",
     "opiv_multipass_create", "opiv_multipass_destroy", "opiv_multipass_window_count",
     "opiv_multipass_grid", "opiv_multipass_process", "opiv_multipass_process_device",
@@ -177,6 +179,10 @@ def load(path: str | None = None) -> C.CDLL:
     L.opiv_batch_get_lanes.argtypes = [C.c_void_p]
     L.opiv_find_peaks.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_uint16, C.c_uint32, _ip, _dp]
     L.opiv_fit_simple_gaussian.argtypes = [_dp, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32, _dp]
+    L.opiv_transform_batch.argtypes = [_dp, C.c_uint32, C.c_int64, C.c_int, _dp, C.c_int]
+    L.opiv_transform_real_batch.argtypes = [_dp, _dp, C.c_uint32, C.c_int64, C.c_int, _dp, _dp, C.c_int]
+    L.opiv_auto_correlate_batch.argtypes = [_dp, C.c_uint32, C.c_int64, _dp, C.c_int]
+    L.opiv_gaussian_offsets.argtypes = [_dp, _dp]
     _lib = L
     return L
 
@@ -550,6 +556,46 @@ def cross_correlate_batch(a: np.ndarray, b: np.ndarray, mode: int, exact: bool =
     _check(load().opiv_cross_correlate_batch(a.ctypes.data_as(_dp), b.ctypes.data_as(_dp), w, n,
                                              mode, int(bool(exact)), out.ctypes.data_as(_dp),
                                              device))
+    return out
+
+
+FORWARD, REVERSE = 0, 1   # algos::direction
+
+
+def _stack(z, dtype):
+    z = np.ascontiguousarray(z, dtype)
+    return z[None] if z.ndim == 2 else z
+
+
+def transform_batch(z: np.ndarray, direction: int = FORWARD, device: int = 0) -> np.ndarray:
+    """FFT::transform (fft.h:87-119) of (n, w, w) or (w, w) complex windows,
+    on the GPU in the reference's double arithmetic."""
+    z = _stack(z, np.complex128)
+    out = np.zeros_like(z)
+    _check(load().opiv_transform_batch(z.ctypes.data_as(_dp), z.shape[-1], z.shape[0], direction,
+                                       out.ctypes.data_as(_dp), device))
+    return out
+
+
+def transform_real_batch(a: np.ndarray, b: np.ndarray, direction: int = FORWARD, device: int = 0):
+    """FFT::transform_real (fft.h:123-186): the two spectra of real windows a, b."""
+    a, b = _stack(a, np.float64), _stack(b, np.float64)
+    if a.shape != b.shape:
+        raise OpivError(ERR_SIZE_MISMATCH, f"image size is different from expected: {a.shape}")
+    oa = np.zeros(a.shape, np.complex128)
+    ob = np.zeros(a.shape, np.complex128)
+    _check(load().opiv_transform_real_batch(a.ctypes.data_as(_dp), b.ctypes.data_as(_dp), a.shape[-1],
+                                            a.shape[0], direction, oa.ctypes.data_as(_dp),
+                                            ob.ctypes.data_as(_dp), device))
+    return oa, ob
+
+
+def auto_correlate_batch(z: np.ndarray, device: int = 0) -> np.ndarray:
+    """FFT::auto_correlate (fft.h:229-242): complex planes, zero imaginary parts."""
+    z = _stack(z, np.complex128)
+    out = np.zeros_like(z)
+    _check(load().opiv_auto_correlate_batch(z.ctypes.data_as(_dp), z.shape[-1], z.shape[0],
+                                            out.ctypes.data_as(_dp), device))
     return out
 
 
