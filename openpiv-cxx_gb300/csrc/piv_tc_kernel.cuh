@@ -252,7 +252,10 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* cst = smem;
     unsigned char* dat = smem + kConstBytes;
-    float* sums = reinterpret_cast<float*>(dat + kDataBytes);          // [window][frame]
+    // pixel sums [window][frame], exact integers: a row sum is an exact
+    // FP32 accumulator value (integer pixels, at most 2^21 for 32 16-bit
+    // pixels); the window sum (up to 2^26) is added in integers
+    int* sums = reinterpret_cast<int*>(dat + kDataBytes);
     int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // window corners
     int* gwi = reinterpret_cast<int*>(org + 2 * kTile);                 // window indices
     float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);              // VT: row sums [frame][row]
@@ -469,7 +472,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         for (int m1 = 0; m1 < 2; ++m1) {
             const float* c = c2 + 32 * m1;
             const int w = 2 * m1 + (warp >> 1), f = warp & 1;
-            float s = (f && (lane & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
+            int s = __float2int_rn(((f && (lane & 1)) ? -c[0] : c[0]) * kSumUnscale);   // undo the frame-B row sign
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) sums[2 * w + f] = s;
@@ -488,9 +491,9 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         __syncthreads();
         if (VT && tid >= 32 && tid < 32 + 2 * kTile) {   // window sums from the row sums
             const int i = (tid - 32) >> 1, f = tid & 1;
-            float s = 0.f;
+            int s = 0;
             if (org[i].x >= 0)
-                for (int yl = 0; yl < W; ++yl) s += rs[f * 64 + i * p.gdy + yl];
+                for (int yl = 0; yl < W; ++yl) s += __float2int_rn(rs[f * 64 + i * p.gdy + yl] * kSumUnscale);
             sums[2 * i + f] = s;
         }
 
@@ -736,7 +739,8 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             __syncwarp();
             // REAL mode: the reference's unpack zeroes spectrum row 0, so its
             // plane has no pedestal
-            const float ped = MODE == kModeReal ? 0.f : (sums[2 * w] * kSumUnscale) * (sums[2 * w + 1] * kSumUnscale);
+            const double ped64 = MODE == kModeReal ? 0.0 : (double)sums[2 * w] * (double)sums[2 * w + 1];
+            const float ped = (float)ped64;
             const int j = lane < 6 ? lane : 0;
             // numerator / denominator positions of lane j's logarithm
             const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
@@ -778,9 +782,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds)
-                    p.peds[gw] = MODE == kModeReal ? 0.0 : (double)(sums[2 * w] * kSumUnscale) *
-                                                           (double)(sums[2 * w + 1] * kSumUnscale);
+                if (p.peds) p.peds[gw] = ped64;
             }
         }
         tcx::fence_before();

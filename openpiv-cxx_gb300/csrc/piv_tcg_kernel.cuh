@@ -165,7 +165,9 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
     unsigned char* cst = smem;
     unsigned char* dat = smem + G::kParts * G::kSet;
     float* xch = reinterpret_cast<float*>(dat + G::kParts * G::kOp);   // exchange rows, then planes
-    float* sums = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(xch) + G::kScratch);
+    // pixel sums [window][frame] as exact integers (row sums are exact FP32
+    // accumulator values for integer pixels; window sums reach 2^28)
+    int* sums = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(xch) + G::kScratch);
     int2* org = reinterpret_cast<int2*>(sums + 2 * WPT);
     int* gwi = reinterpret_cast<int*>(org + WPT);
     unsigned* wmax = reinterpret_cast<unsigned*>(gwi + WPT);
@@ -219,8 +221,8 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             const bool ok = col < p.gnx;
             org[tid] = ok ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy) : make_int2(-1, -1);
             gwi[tid] = row * p.gnx + col;
-            sums[2 * tid] = 0.f;
-            sums[2 * tid + 1] = 0.f;
+            sums[2 * tid] = 0;
+            sums[2 * tid + 1] = 0;
             wmax[tid] = 0u;
         }
         __syncthreads();
@@ -268,7 +270,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             const bool ok = rl < G::R1;
             const int wl = rl / (2 * W), f = (rl / W) & 1, y = rl % W;
             const int wi = m1 * WPM + wl;
-            float s = c[0];
+            int s = __float2int_rn(c[0] * kSumUnscale);
 #pragma unroll
             for (int o = 8; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (ok && (lane & 15) == 0) atomicAdd(&sums[2 * wi + f], s);
@@ -515,7 +517,8 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
                 t1 = n1;
             }
             if (lane == 0) {
-                const float ped = real ? 0.f : (sums[2 * wi] * kSumUnscale) * (sums[2 * wi + 1] * kSumUnscale);
+                const double ped64 = real ? 0.0 : (double)sums[2 * wi] * (double)sums[2 * wi + 1];
+                const float ped = (float)ped64;
                 opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
                 int32_t code = -1;
                 const bool has2 = t1 > TC_NEG_INF;
@@ -548,9 +551,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds)
-                    p.peds[gw] = real ? 0.0 : (double)(sums[2 * wi] * kSumUnscale) *
-                                                  (double)(sums[2 * wi + 1] * kSumUnscale);
+                if (p.peds) p.peds[gw] = ped64;
             }
         }
         tcx::fence_before();

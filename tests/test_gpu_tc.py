@@ -131,6 +131,32 @@ def test_full_pair_split_accuracy():
     assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH, (rms, mx, mm)
 
 
+def full_range_pair(size):
+    """Particle images over the whole 16-bit range (peaks to 65535, clipped):
+    window sums up to 2^26, beyond FP32's exact integers."""
+    return synth.particle_pair(size, size, ppp=0.03, i0_range=(30000, 65000), noise=300.0,
+                               displacement=synth.config2_field, dtype=np.uint16, seed=31,
+                               full_scale=65535.0)
+
+
+@pytest.mark.parametrize("ia,step", [(16, 4), (32, 8), (64, 16)])
+def test_full_range_uint16(ia, step):
+    """16-bit frames over the full range: the split paths' pedestals stay
+    exact (integer window sums, a double product), the planes match numpy's
+    FP64 correlation and the vectors the FP64 pass."""
+    a, b = full_range_pair(512)
+    assert a.max() == 65535
+    ref = run(a, b, step, og.PREC_FP64, ia=ia)
+    for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT_FP16):
+        got = run(a, b, step, precision, planes=True, ia=ia)
+        planes, ped = reference_planes(a, b, got["grid"], ia)
+        assert np.array_equal(got["ped"], ped), "pedestal not exact"
+        err = np.abs(got["planes"] - planes).max(axis=(1, 2)) / np.abs(planes).max(axis=(1, 2))
+        assert err.max() <= 5 * SPLIT_PLANE_RTOL, f"plane error {err.max():.3e} of the plane peak"
+        rms, mx, mm = displacement_error(got, ref)
+        assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH, (precision, rms, mx, mm)
+
+
 def test_limited_search_and_u8():
     a, b = synth.config1()
     ref = run(a, b, 16, og.PREC_FP64, limit=True)
