@@ -138,3 +138,18 @@ def test_vectors_write_format(lib, tmp_path):
     assert lines[0] == "16, 1008, -2.35123, 1.7, 1.23457"
     assert lines[1] == "0, 0, 0, 0, 0"
     assert lines[2] == "48, 1008, nan, -0.25, 10.5"
+
+
+INGEST = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ingest")
+
+
+@pytest.mark.parametrize("name", ["p5_u8", "p5_u16", "p5_u12", "p6_u16", "p6_u8"])
+def test_pnm_equals_reference_loader(lib, name):
+    """opiv_image_load on seeded PNM files against the same files decoded by
+    the reference's own loader (loaders/pnm_image_loader.cpp:199-226,
+    compiled from its sources by tests/golden/make_ingest_golden.py): the
+    16-bit grey samples it hands to the app, value for value."""
+    ref = np.load(os.path.join(os.path.dirname(INGEST), "ingest_ref.npz"))[name]
+    got = og.load_image(os.path.join(INGEST, f"{name}.pnm"))
+    assert got.shape == ref.shape
+    assert np.array_equal(got.astype(np.uint16), ref)
