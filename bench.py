@@ -190,9 +190,18 @@ def cpu_baseline(a, b, grid, budget_s: float = 15.0):
         _, _, t = impl.process_windows(fa, fb, grid[:n], IA, 1, False, threads)
         done += n
         secs += t
+    # the other legs, a shorter sample each: one thread, and the real mode
+    # (FFT::cross_correlate_real) on all threads and on one
+    legs = {"complex_all_threads": done / secs}
+    for name, mode, nt in (("complex_1_thread", 1, 1), ("real_all_threads", 0, threads),
+                           ("real_1_thread", 0, 1)):
+        m = max(200, int(n * nt / threads) // 2)
+        _, _, t = impl.process_windows(fa, fb, grid[:m], IA, mode, False, nt)
+        legs[name] = m / max(t, 1e-9)
     return {"value": done / secs, "unit": METRIC, "cores": threads, "kind": kind,
             "sample": f"{done} windows ({n} per run, first rows of the {len(grid)}-window grid), "
-                      f"complex mode, {threads} threads, {secs:.1f} s"}
+                      f"complex mode, {threads} threads, {secs:.1f} s",
+            "legs": legs}
 
 
 # executed tensor-core FLOPs per 32 x 32 window of the DFT-GEMM kernel
@@ -869,7 +878,7 @@ def run_reference(args):
     # size each step so that warmup + steps take about two minutes
     _, _, t = impl.process_windows(fa, fb, grid[:2000], IA, 1, False, threads)
     rate = 2000 / max(t, 1e-6)
-    per_step = int(min(len(grid), max(1000, rate * 120.0 / max(1, args.steps + args.warmup))))
+    per_step = int(min(len(grid), max(1000, rate * args.reference_seconds / max(1, args.steps + args.warmup))))
     for _ in range(args.warmup):
         impl.process_windows(fa, fb, grid[:per_step], IA, 1, False, threads)
     secs = 0.0
@@ -885,11 +894,27 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded particle images, 0.03 ppp, 12-bit)", "impl": "reference",
         "config": {"workload": WORKLOAD, "windows_per_step": per_step, "ia": IA, "step": STEP,
-                   "mode": "complex (FFT::cross_correlate)"},
+                   "mode": "complex (FFT::cross_correlate)",
+                   "ranks": int(os.environ.get("WORLD_SIZE", "1")),
+                   "note": "the reference is a CPU library: rank 0 runs it, the other ranks exit"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def launch_replicas(n: int, argv: list[str]) -> int:
+    """`--gpus N` outside a torchrun launch: N ranks on this node, one per
+    GPU, by re-running this script under torch.distributed.run (rendezvous
+    on 127.0.0.1, a free port); returns the launcher's exit status."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + argv
+    return subprocess.call(cmd)
 
 
 def main():
@@ -907,7 +932,11 @@ def main():
     ap.add_argument("--mc-seeds", type=int, default=1000, help="Monte Carlo seeds of the adjoint workload")
     ap.add_argument("--sweep-size", type=int, default=2048,
                     help="image size of the precision sweep")
+    ap.add_argument("--reference-seconds", type=float, default=120.0,
+                    help="CPU seconds of the reference arm's warm-up plus timed steps")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_replicas(args.gpus, sys.argv[1:]))
     if args.steps is None:
         args.steps = 20 if args.workload == "batch" and args.impl == "ours" else 1000
     args.warmup = max(3, args.warmup)
