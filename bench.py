@@ -358,7 +358,7 @@ def run_ours(args):
     # the other tensor-core precisions: throughput (a shorter run) and accuracy
     others = {}
     for name, prec in (("tc_bf16", og.PREC_TC_BF16), ("tc_split_fp16", og.PREC_TC_SPLIT_FP16),
-                       ("tc_fp16", og.PREC_TC_FP16)):
+                       ("tc_fp16", og.PREC_TC_FP16), ("tc_split2_fp16", og.PREC_TC_SPLIT2_FP16)):
         n_o = max(3, args.steps // 10)
         el, ms, _, _, v, k, _ = timed(prec, n_o, 3)
         others[name] = {"value": n_o * N_WIN * world / el, "kernel_ms": statistics.mean(ms)}

@@ -117,7 +117,16 @@ int exact_all_blocks(int device) { return 8 * device_sm_count(device); }
 bool is_tc(int precision)
 {
     return precision == OPIV_PREC_TC_SPLIT_BF16 || precision == OPIV_PREC_TC_BF16 ||
-           precision == OPIV_PREC_TC_SPLIT_FP16 || precision == OPIV_PREC_TC_FP16;
+           precision == OPIV_PREC_TC_SPLIT_FP16 || precision == OPIV_PREC_TC_FP16 ||
+           precision == OPIV_PREC_TC_SPLIT2_FP16;
+}
+
+// MMAs per product of a tensor-core precision: 3 (hi*hi + hi*lo + lo*hi),
+// 2 (data split, constants single) or 1
+int tc_passes(int precision)
+{
+    if (precision == OPIV_PREC_TC_SPLIT_BF16 || precision == OPIV_PREC_TC_SPLIT_FP16) return 3;
+    return precision == OPIV_PREC_TC_SPLIT2_FP16 ? 2 : 1;
 }
 
 // The PocketFFT modes compute the true circular correlation, as
@@ -316,9 +325,9 @@ int run_pass(opiv_plan* p, const void* fa, const void* fb, size_t pitch, opiv_ve
         k.tc_tile = p->tc_tile;
         k.mma_skip = p->mma_skip;
         if (p->timing) CUDA_TRY(cudaEventRecord(p->ev[0], s));
-        CUDA_TRY(launch_piv_tc(k, (int)p->ia, p->dtype, p->mode, p->limit,
-                               p->precision == OPIV_PREC_TC_SPLIT_BF16 || p->precision == OPIV_PREC_TC_SPLIT_FP16,
-                               p->precision == OPIV_PREC_TC_SPLIT_FP16 || p->precision == OPIV_PREC_TC_FP16,
+        CUDA_TRY(launch_piv_tc(k, (int)p->ia, p->dtype, p->mode, p->limit, tc_passes(p->precision),
+                               p->precision == OPIV_PREC_TC_SPLIT_FP16 || p->precision == OPIV_PREC_TC_FP16 ||
+                                   p->precision == OPIV_PREC_TC_SPLIT2_FP16,
                                p->d_tc, s));
         ++g_launches;
         if (p->timing) {
@@ -503,7 +512,7 @@ int opiv_plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype,
 int opiv_plan_create_tc(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
                         uint32_t dx, uint32_t dy, int mode, int limit_search, int precision, int device)
 {
-    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_FP16)
+    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_SPLIT2_FP16)
         return fail(OPIV_ERR_ARG, "unknown precision %d", precision);
     if (!is_tc(precision)) return fail(OPIV_ERR_ARG, "precision %d is not a tensor-core precision", precision);
     int rc = plan_create(out, img_w, img_h, dtype, ia, dx, dy, mode, limit_search, device, true);
@@ -1669,7 +1678,7 @@ int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_
 int opiv_plan_set_precision(opiv_plan* plan, int precision)
 {
     if (!plan) return fail(OPIV_ERR_ARG, "plan is null");
-    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_FP16)
+    if (precision < OPIV_PREC_FP32 || precision > OPIV_PREC_TC_SPLIT2_FP16)
         return fail(OPIV_ERR_ARG, "unknown precision %d", precision);
     if (!is_tc(precision) && !is_pow2(plan->ia))
         return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", plan->ia, plan->ia);
@@ -1677,6 +1686,8 @@ int opiv_plan_set_precision(opiv_plan* plan, int precision)
         if (!tc_supports((int)plan->ia, plan->dtype))
             return fail(OPIV_ERR_UNSUPPORTED,
                         "the tensor-core path takes 16, 32, 48 or 64 px windows of u8/u16 frames");
+        if (precision == OPIV_PREC_TC_SPLIT2_FP16 && plan->ia != 32)
+            return fail(OPIV_ERR_UNSUPPORTED, "the two-MMA split precision takes 32 px windows");
         if (plan->ia == 32 && (plan->g.xs % 8 != 0 || plan->dx % 8 != 0))
             return fail(OPIV_ERR_UNSUPPORTED,
                         "the 32 px tensor-core path needs window x positions on multiples of 8 pixels");

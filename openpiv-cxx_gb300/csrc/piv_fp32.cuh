@@ -398,7 +398,9 @@ __device__ __forceinline__ void fp32_task(const PivParams& p, const int task, fl
             const float dn = v[(y + 1) & (W - 1)].x;
             const float lf = __shfl_sync(0xffffffffu, c, (gl + W - 1) & (W - 1), W);
             const float rt = __shfl_sync(0xffffffffu, c, (gl + 1) & (W - 1), W);
-            const float dd = fmaxf(fmaxf(up, dn), fmaxf(lf, rt)) - c;
+            float m4;   // max of the four neighbours (a three-source max and a max)
+            asm("max.f32 %0, %1, %2, %3;" : "=f"(m4) : "f"(up), "f"(dn), "f"(fmaxf(lf, rt)));
+            const float dd = m4 - c;
             const bool strict = col_ok && (dd < 0.f);
             const bool unc = col_ok && (fabsf(dd) <= dlt);
             umax = unc ? fmaxf(umax, c) : umax;

@@ -69,8 +69,10 @@ cudaError_t launch_piv_adjoint(const PivParams& p, int w, int dtype, const int32
                                const float* cot, float* grad_a, float* grad_b, size_t gpitch,
                                float var_a, float var_b, float* sigma, cudaStream_t s);
 
-// consts: tc_constant_bytes(w) bytes from tc_constants (BF16 set, FP16 set)
-cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int limit, bool split,
+// consts: tc_constant_bytes(w) bytes from tc_constants (BF16 set, FP16 set);
+// passes: MMAs per product, 3 (hi*hi + hi*lo + lo*hi), 2 (data split,
+// constants single; 32 px windows) or 1
+cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int limit, int passes,
                           bool fp16, const void* consts, cudaStream_t s);
 
 // Fused FP32 kernels, one entry per window size (piv_fp32_w*.cu; 64 x 64

@@ -146,28 +146,28 @@ __device__ __forceinline__ void put1(unsigned char* base, int off, float v)
     }
 }
 
-// D (+)= A * B with hi/lo splitting: hi*hi, then hi*lo and lo*hi.  a and b
-// are descriptors of the hi parts; the start-address field counts 16-byte
-// units, so a byte offset o is added as o >> 4 (no carry: shared addresses
-// are below 2^18).
-template <bool SPLIT>
+// D (+)= A * B with hi/lo splitting: hi*hi, then hi*lo (CSPLIT: the
+// constant's lo part) and lo*hi.  a and b are descriptors of the hi parts;
+// the start-address field counts 16-byte units, so a byte offset o is added
+// as o >> 4 (no carry: shared addresses are below 2^18).
+template <bool SPLIT, bool CSPLIT>
 __device__ __forceinline__ void mma3(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, bool acc)
 {
     tcx::mma_bf16(d, a, b, idesc, acc);
     if (SPLIT) {
-        tcx::mma_bf16(d, a, b + ((kTcNumMat * kMat) >> 4), idesc, true);
+        if (CSPLIT) tcx::mma_bf16(d, a, b + ((kTcNumMat * kMat) >> 4), idesc, true);
         tcx::mma_bf16(d, a + (kLo >> 4), b, idesc, true);
     }
 }
 
 // The same with the A operand (hi part a_hi, lo part a_lo) in tensor memory.
-template <bool SPLIT>
+template <bool SPLIT, bool CSPLIT>
 __device__ __forceinline__ void mma3_ta(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint64_t b, uint32_t idesc,
                                         bool acc)
 {
     tcx::mma_bf16_ta(d, a_hi, b, idesc, acc);
     if (SPLIT) {
-        tcx::mma_bf16_ta(d, a_hi, b + ((kTcNumMat * kMat) >> 4), idesc, true);
+        if (CSPLIT) tcx::mma_bf16_ta(d, a_hi, b + ((kTcNumMat * kMat) >> 4), idesc, true);
         tcx::mma_bf16_ta(d, a_lo, b, idesc, true);
     }
 }
@@ -227,7 +227,9 @@ __device__ __forceinline__ void widen8<uint8_t>(const uint2& q, float* px, float
 // (pixels x 2^-4, the stage-1 matrix x 2^-9 in the constants, the
 // product x 2^-e with e chosen per window from its largest value, T x
 // 2^-6), undone exactly in the peak stage.
-template <bool F16, bool SPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
+// CSPLIT: the constants' lo parts enter too (three MMAs per product);
+// otherwise only the data is split (two).
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
 __global__ void __launch_bounds__(kThreads, 4)
 piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 {
@@ -400,7 +402,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             for (int m1 = 0; m1 < NM; ++m1)
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
-                    mma3_ta<SPLIT>(tbase + 32 * m1, tbase + kA1 + 16 * m1 + 8 * ks,
+                    mma3_ta<SPLIT, CSPLIT>(tbase + 32 * m1, tbase + kA1 + 16 * m1 + 8 * ks,
                                    tbase + kA1 + 16 * NM + 16 * m1 + 8 * ks, mat(kTcG1, ks), kIdK32, ks > 0);
             tcx::commit(mbar);
         }
@@ -503,7 +505,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dA2 + off(ks * 4096), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdM64,
+                mma3<SPLIT, CSPLIT>(tbase, dA2 + off(ks * 4096), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdM64,
                             ks > 0);
             tcx::commit(mbar);
         }
@@ -626,30 +628,28 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dA3 + off(ks * 256), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdK64M64,
+                mma3<SPLIT, CSPLIT>(tbase, dA3 + off(ks * 256), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdK64M64,
                             ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
 
         // ---- E3: T into the stage-4 operand (MN-major, rows (window, y') =
-        // 128, K = (Re | Im) x k_x = 32); warp w, lanes 0..15 = k_x
+        // 128, K = (Re | Im) x k_x = 32); warp w: its window's 16 rows
+        // (k_x) sit in lanes 0..15, so lane = part * 16 + k_x takes the Re
+        // (part 0) or Im (part 1) half of row k_x
         {
-            const int w = warp, kxr = lane;
-            float t2[64];
-            tcx::tmem_ld32x2(tlane, tlane + 32, t2, t2 + 32);
+            const int w = warp, part = lane >> 4, kxr = lane & 15;
+            float t1[32];
+            tcx::tmem_ld16x2_32(tlane, t1);
             if (F16) {
 #pragma unroll
-                for (int i = 0; i < 64; ++i) t2[i] *= kT;
+                for (int i = 0; i < 32; ++i) t1[i] *= kT;
             }
-            if (lane < 16)
+            const int k = part * 16 + kxr;
+            const int base = (k >> 3) * 2048 + (k & 7) * 16;
 #pragma unroll
-            for (int part = 0; part < 2; ++part) {
-                const int k = part * 16 + kxr;
-                const int base = (k >> 3) * 2048 + (k & 7) * 16;
-#pragma unroll
-                for (int g = 0; g < 4; ++g) put8<F16, SPLIT>(dat, base + (w * 4 + g) * 128, t2 + 32 * part + 8 * g);
-            }
+            for (int g = 0; g < 4; ++g) put8<F16, SPLIT>(dat, base + (w * 4 + g) * 128, t1 + 8 * g);
         }
         tcx::fence_proxy();
         tcx::fence_before();
@@ -660,7 +660,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 2; ++ks)
-                mma3<SPLIT>(tbase, dA2 + off(ks * 4096), mat(kTcC4, ks), kIdM32, ks > 0);
+                mma3<SPLIT, CSPLIT>(tbase, dA2 + off(ks * 4096), mat(kTcC4, ks), kIdM32, ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -690,7 +690,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                     const float c = v[x];
                     const float up = __shfl_up_sync(0xffffffffu, c, 1);
                     const float dn = __shfl_down_sync(0xffffffffu, c, 1);
-                    const float m = fmaxf(fmaxf(up, dn), fmaxf(v[x - 1], v[x + 1]));
+                    const float m = tcx::fmax3(up, dn, fmaxf(v[x - 1], v[x + 1]));
                     T0[x - SX0] = (m < c) ? c : TC_NEG_INF;
                     T1[x - SX0] = TC_NEG_INF;
                     I0[x - SX0] = x;
@@ -701,7 +701,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                     for (int i = 0; i + st < NX; i += 2 * st) {
                         const bool gt = T0[i + st] > T0[i];
                         const float lo = fminf(T0[i], T0[i + st]);
-                        T1[i] = fmaxf(fmaxf(T1[i], T1[i + st]), lo);
+                        T1[i] = tcx::fmax3(T1[i], T1[i + st], lo);
                         I0[i] = gt ? I0[i + st] : I0[i];
                         T0[i] = gt ? T0[i + st] : T0[i];
                     }
@@ -794,10 +794,10 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     if (warp == 0) tcx::tmem_dealloc(tbase, kTmemCols);
 }
 
-template <bool F16, bool SPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
 cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
 {
-    auto kern = piv_tc_kernel<F16, SPLIT, MODE, LIMIT, PixT, VT>;
+    auto kern = piv_tc_kernel<F16, SPLIT, CSPLIT, MODE, LIMIT, PixT, VT>;
     static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
     static std::atomic<int> sm_count[64];
     int dev = 0;
@@ -822,27 +822,28 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
     return cudaGetLastError();
 }
 
-template <bool F16, bool SPLIT, int MODE, bool LIMIT>
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT>
 cudaError_t by_dtype(const PivParams& p, int dtype, const void* consts, cudaStream_t s)
 {
     // four stacked windows span <= 56 rows; the plan may ask for row tiles
     const bool vt = p.tc_tile != 2 && p.gdy > 0 && p.gdy <= 8;
     if (dtype == kU8)
-        return vt ? launch_t<F16, SPLIT, MODE, LIMIT, uint8_t, true>(p, consts, s)
-                  : launch_t<F16, SPLIT, MODE, LIMIT, uint8_t, false>(p, consts, s);
-    return vt ? launch_t<F16, SPLIT, MODE, LIMIT, uint16_t, true>(p, consts, s)
-              : launch_t<F16, SPLIT, MODE, LIMIT, uint16_t, false>(p, consts, s);
+        return vt ? launch_t<F16, SPLIT, CSPLIT, MODE, LIMIT, uint8_t, true>(p, consts, s)
+                  : launch_t<F16, SPLIT, CSPLIT, MODE, LIMIT, uint8_t, false>(p, consts, s);
+    return vt ? launch_t<F16, SPLIT, CSPLIT, MODE, LIMIT, uint16_t, true>(p, consts, s)
+              : launch_t<F16, SPLIT, CSPLIT, MODE, LIMIT, uint16_t, false>(p, consts, s);
 }
 
-template <bool F16, bool SPLIT>
+// SPLIT: hi / lo data (and, with CSPLIT, constant) parts
+template <bool F16, bool SPLIT, bool CSPLIT = SPLIT>
 cudaError_t by_mode(const PivParams& p, int dtype, int mode, int limit, const void* consts,
                     cudaStream_t s)
 {
     if (mode == kModeReal)
-        return limit ? by_dtype<F16, SPLIT, kModeReal, true>(p, dtype, consts, s)
-                     : by_dtype<F16, SPLIT, kModeReal, false>(p, dtype, consts, s);
-    return limit ? by_dtype<F16, SPLIT, kModeComplex, true>(p, dtype, consts, s)
-                 : by_dtype<F16, SPLIT, kModeComplex, false>(p, dtype, consts, s);
+        return limit ? by_dtype<F16, SPLIT, CSPLIT, kModeReal, true>(p, dtype, consts, s)
+                     : by_dtype<F16, SPLIT, CSPLIT, kModeReal, false>(p, dtype, consts, s);
+    return limit ? by_dtype<F16, SPLIT, CSPLIT, kModeComplex, true>(p, dtype, consts, s)
+                 : by_dtype<F16, SPLIT, CSPLIT, kModeComplex, false>(p, dtype, consts, s);
 }
 
 }  // namespace tc

@@ -39,7 +39,7 @@ ERR_CUDA = -12
 ERR_NO_DEVICE = -13
 ERR_TIMEOUT = -14
 PREC_FP32, PREC_TC_SPLIT_BF16, PREC_TC_BF16, PREC_FP64 = 0, 1, 2, 3
-PREC_TC_SPLIT_FP16, PREC_TC_FP16 = 4, 5
+PREC_TC_SPLIT_FP16, PREC_TC_FP16, PREC_TC_SPLIT2_FP16 = 4, 5, 6
 
 DTYPES = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
 SYMBOLS = [

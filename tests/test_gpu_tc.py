@@ -18,7 +18,10 @@ SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH = 1e-4, 1e-3, 1e-4
 BF16_RMS, BF16_MAX, BF16_MISMATCH = 0.01, 0.05, 5e-3
 # plain FP16 (11-bit significand, scaled): between the two
 FP16_RMS, FP16_MAX, FP16_MISMATCH = 1e-3, 1e-2, 1e-3
+# FP16 data split into hi + lo, FP16 constants single: the constants' rounding
+SPLIT2_RMS, SPLIT2_MAX, SPLIT2_MISMATCH = 1e-3, 1e-2, 1e-3
 BOUNDS = {og.PREC_TC_SPLIT_BF16: (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH),
+          og.PREC_TC_SPLIT2_FP16: (SPLIT2_RMS, SPLIT2_MAX, SPLIT2_MISMATCH),
           og.PREC_TC_BF16: (BF16_RMS, BF16_MAX, BF16_MISMATCH),
           og.PREC_TC_SPLIT_FP16: (SPLIT_RMS, SPLIT_MAX, SPLIT_MISMATCH),
           og.PREC_TC_FP16: (FP16_RMS, FP16_MAX, FP16_MISMATCH)}
@@ -99,7 +102,8 @@ def displacement_error(got, ref):
 @pytest.mark.parametrize("precision,rtol", [(og.PREC_TC_SPLIT_BF16, SPLIT_PLANE_RTOL),
                                             (og.PREC_TC_BF16, 1e-2),
                                             (og.PREC_TC_SPLIT_FP16, SPLIT_PLANE_RTOL),
-                                            (og.PREC_TC_FP16, 2e-3)])
+                                            (og.PREC_TC_FP16, 2e-3),
+                                            (og.PREC_TC_SPLIT2_FP16, 1e-3)])
 def test_planes_match_fp64_fft(precision, rtol):
     a, b = synth.config1()
     got = run(a, b, 16, precision, planes=True)
@@ -182,6 +186,9 @@ def test_precision_argument_errors():
     p16 = og.Plan(260, 256, np.uint16, 16, 8)
     assert p16.grid()[0, 0] == 2
     p16.set_precision(og.PREC_TC_SPLIT_BF16)
+    with pytest.raises(og.OpivError) as e:     # the two-MMA split: 32 px windows only
+        p16.set_precision(og.PREC_TC_SPLIT2_FP16)
+    assert e.value.status == og.ERR_UNSUPPORTED
     pf = og.Plan(256, 256, np.float32, 32, 8)
     with pytest.raises(og.OpivError) as e:
         pf.set_precision(og.PREC_TC_BF16)
@@ -242,6 +249,8 @@ def test_generic_vectors_against_fp64(ia, step, orc):
     a, b = synth.config2(size=1024)
     ref = fp64_reference(a, b, step, ia, og.CORR_COMPLEX, orc) if ia == 48 else run(a, b, step, og.PREC_FP64, ia=ia)
     for precision, (rms_t, max_t, mm_t) in BOUNDS.items():
+        if precision == og.PREC_TC_SPLIT2_FP16:   # 32 px windows only
+            continue
         got = run(a, b, step, precision, ia=ia)
         assert np.array_equal(got["grid"], ref["grid"])
         rms, mx, mm = displacement_error(got, ref)
