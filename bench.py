@@ -65,8 +65,9 @@ METRIC = "vectors/s"
 WORKLOAD = f"piv_pair_{IMG}x{IMG}_u16_ia{IA}_step{STEP}"
 L2_ROTATION = 4
 # DRAM bytes (read + write) of one launch of the timed kernels on this
-# workload, from ncu captures (the bench cannot profile itself)
-TC_TRAFFIC_BYTES = 69_884_160 + 3_193_344
+# workload, from ncu captures of the current kernels (the bench cannot
+# profile itself; recaptured whenever a kernel changes)
+TC_TRAFFIC_BYTES = 69_602_816 + 3_013_888
 FP32_TRAFFIC_BYTES = 67_200_000 + 3_700_000
 
 
@@ -578,6 +579,7 @@ def run_batch(args):
         batch.process_into(*ptrs)
 
     e2e_steps = max(5, args.steps // 4)
+    call_ms = {}
 
     def e2e_time(schedule):
         batch.set_schedule(schedule)
@@ -587,9 +589,28 @@ def run_batch(args):
         e2e_step()
         dist_barrier(world)
         t0 = time.perf_counter()
+        per = []
         for _ in range(e2e_steps):
+            t1 = time.perf_counter()
             e2e_step()
+            per.append((time.perf_counter() - t1) * 1e3)
+        call_ms[schedule] = per
         return dist_max(time.perf_counter() - t0, world)
+
+    # the host-to-device bandwidth of these pinned frames, one stream, timed
+    # on the device (the upload is most of an end-to-end call's copies)
+    dev_frames = [(torch.empty_like(a, device=dev), torch.empty_like(b, device=dev)) for a, b in pinned]
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for rep in range(2):
+            ev0.record(stream)
+            for (da, db), (a, b) in zip(dev_frames, pinned):
+                da.copy_(a, non_blocking=True)
+                db.copy_(b, non_blocking=True)
+            ev1.record(stream)
+    stream.synchronize()
+    h2d_gbs = h2d / (ev0.elapsed_time(ev1) / 1e3) / 1e9
+    del dev_frames
 
     t_e2e_streams = e2e_time(og.BATCH_STREAMS)
     t_e2e_queue = e2e_time(og.BATCH_QUEUE)
@@ -643,7 +664,10 @@ def run_batch(args):
                          "opiv_batch_process, queue schedule (all uploads, the queue graph, "
                          "all downloads)"),
                 "streams": e2e_steps * final * world / t_e2e_streams,
-                "queue": e2e_steps * final * world / t_e2e_queue},
+                "queue": e2e_steps * final * world / t_e2e_queue,
+                "call_ms_streams": [round(x, 2) for x in call_ms[og.BATCH_STREAMS]],
+                "call_ms_queue": [round(x, 2) for x in call_ms[og.BATCH_QUEUE]],
+                "pinned_h2d_gbs": h2d_gbs},
         "gpu_launches": gpu_launches,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
