@@ -58,11 +58,25 @@ constexpr int kThreads = 128;
 constexpr int kTile = 4;                        // windows per tile
 constexpr int kMat = 2048;                      // one 32 x 32 BF16 matrix, K-major
 constexpr int kConstBytes = kTcNumMat * 2 * kMat;
-constexpr int kDataBytes = 34 * 1024;
+constexpr int kDataBytes = 32 * 1024;   // stage-2 operand, hi and lo parts (its largest user)
 constexpr int kTailBytes = 768;                 // sums, origins, indices, row sums, mbarrier, TMEM slot, flag
 constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
 constexpr uint32_t kTmemCols = 128;
 constexpr uint32_t kA1 = 64;                    // TMEM column of the stage-1 operand (hi, then lo)
+// Grouped form (vertical tiles): one CTA per SM runs kGroups independent
+// groups of 4 warps, each doing what one CTA of the plain form does, sharing
+// one copy of the constant matrices; a group has 64 tensor-memory columns
+// (stage-1 accumulator in 0..31, its pixel operand in 32..63, later stages'
+// accumulators in 0..63) and its own data buffer, tail, mbarrier and named
+// barrier.  Six groups fit the SM's registers (768 threads at 80 each),
+// shared memory and tensor memory, against four CTAs of the plain form.
+constexpr int kGroups = 6;
+constexpr uint32_t kGroupCols = 64;
+constexpr uint32_t kA1Grouped = 32;
+constexpr int kGroupBytes = (kDataBytes + kTailBytes + 1023) / 1024 * 1024;
+constexpr int kSmemGrouped = kConstBytes + kGroups * kGroupBytes;
+static_assert(kSmemGrouped <= 227 * 1024, "grouped form: shared memory");
+static_assert(kGroups * kGroupCols <= 512, "grouped form: tensor memory");
 constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
 constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (after the stage-3 operand)
 constexpr int kPRow = 36;                       // E4 plane row (floats), padded
@@ -229,10 +243,17 @@ __device__ __forceinline__ void widen8<uint8_t>(const uint2& q, float* px, float
 // 2^-6), undone exactly in the peak stage.
 // CSPLIT: the constants' lo parts enter too (three MMAs per product);
 // otherwise only the data is split (two).
-template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
-__global__ void __launch_bounds__(kThreads, 4)
+// GROUPS: 1 (one tile group per CTA, four CTAs per SM) or kGroups (the
+// grouped form, vertical tiles only).
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT, bool VT, int GROUPS>
+__global__ void __launch_bounds__(kThreads * GROUPS, GROUPS == 1 ? 4 : 1)
 piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 {
+    static_assert(GROUPS == 1 || VT, "the grouped form takes vertical tiles");
+    // tensor-memory columns: the stage-1 operand's first column, the CTA's
+    // allocation
+    constexpr uint32_t A1 = GROUPS == 1 ? kA1 : kA1Grouped;
+    constexpr uint32_t kCols = GROUPS == 1 ? kTmemCols : 512;
     // peak scan range in swapped-plane coordinates (image_utils.impl.h:48,
     // :54; limited search: rect::dilate(0.5), rect.cpp:109-126)
     constexpr int D0 = LIMIT ? W / 4 : 0;
@@ -253,7 +274,9 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* cst = smem;
-    unsigned char* dat = smem + kConstBytes;
+    // this thread's tile group: its data buffer and tail
+    const int grp = GROUPS == 1 ? 0 : (int)(threadIdx.x / kThreads);
+    unsigned char* dat = smem + kConstBytes + (GROUPS == 1 ? 0 : grp * kGroupBytes);
     // pixel sums [window][frame], exact integers: a row sum is an exact
     // FP32 accumulator value (integer pixels, at most 2^21 for 32 16-bit
     // pixels); the window sum (up to 2^26) is added in integers
@@ -265,8 +288,17 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
     int* abort_flag = reinterpret_cast<int*>(tslot + 1);
     int* escale = abort_flag + 1;                                       // F16: product exponent per window
+    // the CTA's tensor-memory address lives in group 0's tail
+    uint32_t* tslot_cta =
+        reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(tslot) - (dat - (smem + kConstBytes)));
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // thread, warp and lane within the tile group (warp w of a group reads
+    // tensor-memory lanes 32w .. 32w + 31, the quarter of CTA warp 4g + w)
+    const int tid = (int)threadIdx.x % kThreads, warp = tid >> 5, lane = tid & 31;
+    auto gsync = [&]() {
+        if constexpr (GROUPS == 1) __syncthreads();
+        else asm volatile("bar.sync %0, %1;" :: "r"(1 + grp), "r"(kThreads) : "memory");
+    };
     const uint32_t cst_a = tcx::smem_addr(cst), dat_a = tcx::smem_addr(dat);
     // descriptors: constant matrix m (hi part; the lo parts follow all hi
     // parts), and the data buffer in the layouts of the four stages
@@ -276,17 +308,18 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     const uint64_t dA3 = tcx::sdesc(dat_a, 128, 1024);    // K-major, 8 k-groups per row group
     auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
 
-    for (int i = tid; i < kConstBytes / 16; i += kThreads)
+    for (int i = threadIdx.x; i < kConstBytes / 16; i += kThreads * GROUPS)
         reinterpret_cast<uint4*>(cst)[i] = consts[i];
     if (tid == 0) {
         tcx::mbar_init(mbar, 1);
         *abort_flag = 0;
     }
-    if (warp == 0) tcx::tmem_alloc(tslot, kTmemCols);
+    if (threadIdx.x < 32) tcx::tmem_alloc(tslot_cta, kCols);
     tcx::fence_before();
     __syncthreads();
     tcx::fence_after();
-    const uint32_t tbase = *tslot;
+    const uint32_t tcta = *tslot_cta;
+    const uint32_t tbase = tcta + (uint32_t)grp * kGroupCols;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
 
     const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
@@ -300,8 +333,10 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     const int n_line = VT ? p.gnx : gny;
     const int per_line = VT ? (gny + kTile - 1) / kTile : (p.gnx + kTile - 1) / kTile;
     const int n_tiles = n_line * per_line;
-    const int t_begin = (int)((int64_t)blockIdx.x * n_tiles / gridDim.x);
-    const int t_end = (int)((int64_t)(blockIdx.x + 1) * n_tiles / gridDim.x);
+    // each tile group walks its own contiguous range
+    const int64_t vb = (int64_t)blockIdx.x * GROUPS + grp, vg = (int64_t)gridDim.x * GROUPS;
+    const int t_begin = (int)(vb * n_tiles / vg);
+    const int t_end = (int)((vb + 1) * n_tiles / vg);
     uint32_t phase = 0;
 
     // wait for the committed MMAs; a wait that gives up aborts the CTA
@@ -336,7 +371,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             org[tid] = ok ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy) : make_int2(-1, -1);
             gwi[tid] = row * p.gnx + col;
         }
-        __syncthreads();
+        gsync();
 
         // number of window rows of this tile (VT: image rows below its top)
         const int vrows = VT ? (org[1].x >= 0 ? (org[2].x >= 0 ? (org[3].x >= 0 ? 3 : 2) : 1) : 0) * p.gdy + W
@@ -384,13 +419,13 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                         }
                     }
                 }
-                tcx::tmem_st16(tlane + kA1 + 16 * m1, hw);
-                if (SPLIT) tcx::tmem_st16(tlane + kA1 + 16 * NM + 16 * m1, lw);
+                tcx::tmem_st16(tlane + A1 + 16 * m1, hw);
+                if (SPLIT) tcx::tmem_st16(tlane + A1 + 16 * NM + 16 * m1, lw);
             }
         }
         tcx::fence_proxy();
         tcx::fence_before();
-        __syncthreads();
+        gsync();
         if (*abort_flag) break;
 
         // ---- stage 1: H = X * G, one (VT) or two M-tiles of 128 rows, the
@@ -402,8 +437,8 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             for (int m1 = 0; m1 < NM; ++m1)
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
-                    mma3_ta<SPLIT, CSPLIT>(tbase + 32 * m1, tbase + kA1 + 16 * m1 + 8 * ks,
-                                   tbase + kA1 + 16 * NM + 16 * m1 + 8 * ks, mat(kTcG1, ks), kIdK32, ks > 0);
+                    mma3_ta<SPLIT, CSPLIT>(tbase + 32 * m1, tbase + A1 + 16 * m1 + 8 * ks,
+                                   tbase + A1 + 16 * NM + 16 * m1 + 8 * ks, mat(kTcG1, ks), kIdK32, ks > 0);
             tcx::commit(mbar);
         }
         // the next tile's window rows into L2 while this tile computes
@@ -490,7 +525,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         tcx::fence_proxy();
         tcx::fence_before();
-        __syncthreads();
+        gsync();
         if (VT && tid >= 32 && tid < 32 + 2 * kTile) {   // window sums from the row sums
             const int i = (tid - 32) >> 1, f = tid & 1;
             int s = 0;
@@ -620,7 +655,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         tcx::fence_proxy();
         tcx::fence_before();
-        __syncthreads();
+        gsync();
 
         // ---- stage 3: inverse column DFT, Re T = Pr*C + Pi*(-S),
         // Im T = Pr*S + Pi*C (M = 64)
@@ -653,7 +688,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         tcx::fence_proxy();
         tcx::fence_before();
-        __syncthreads();
+        gsync();
 
         // ---- stage 4: real inverse row DFT, D = T * C4
         if (tid == 0 && !p.mma_skip) {
@@ -786,25 +821,29 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             }
         }
         tcx::fence_before();
-        __syncthreads();
+        gsync();
     }
     tcx::fence_before();
     __syncthreads();
     tcx::fence_after();
-    if (warp == 0) tcx::tmem_dealloc(tbase, kTmemCols);
+    if (threadIdx.x < 32) tcx::tmem_dealloc(tcta, kCols);
 }
 
 template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT, bool VT>
 cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
 {
-    auto kern = piv_tc_kernel<F16, SPLIT, CSPLIT, MODE, LIMIT, PixT, VT>;
+    // vertical tiles run the grouped form (one CTA of kGroups tile groups
+    // per SM), row tiles the plain form (four CTAs per SM)
+    constexpr int G = VT ? kGroups : 1;
+    constexpr int kSmem = G == 1 ? kSmemBytes : kSmemGrouped;
+    auto kern = piv_tc_kernel<F16, SPLIT, CSPLIT, MODE, LIMIT, PixT, VT, G>;
     static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
     static std::atomic<int> sm_count[64];
     int dev = 0;
     cudaGetDevice(&dev);
     const uint64_t bit = 1ull << (dev & 63);
     if (!(attr_done.load() & bit)) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
         if (e != cudaSuccess) return e;
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -815,10 +854,12 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
     const int64_t gny = p.n_win / p.gnx;
     const int64_t tiles = VT ? (int64_t)p.gnx * ((gny + kTile - 1) / kTile)
                              : gny * ((p.gnx + kTile - 1) / kTile);
-    const int64_t cap = 4 * (int64_t)sm_count[dev & 63].load();
-    const int blocks = (int)(tiles < cap ? tiles : cap);
+    // four CTAs per SM (plain form) or one (grouped form)
+    const int64_t cap = (G == 1 ? 4 : 1) * (int64_t)sm_count[dev & 63].load();
+    const int64_t want = (tiles + G - 1) / G;
+    const int blocks = (int)(want < cap ? want : cap);
     if (blocks <= 0) return cudaSuccess;
-    kern<<<blocks, kThreads, kSmemBytes, s>>>(p, reinterpret_cast<const uint4*>(consts));
+    kern<<<blocks, kThreads * G, kSmem, s>>>(p, reinterpret_cast<const uint4*>(consts));
     return cudaGetLastError();
 }
 
