@@ -774,8 +774,10 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             __syncwarp();
             // REAL mode: the reference's unpack zeroes spectrum row 0, so its
             // plane has no pedestal
-            const double ped64 = MODE == kModeReal ? 0.0 : (double)sums[2 * w] * (double)sums[2 * w + 1];
-            const float ped = (float)ped64;
+            // the pedestal for the fit in FP32 (the exact integer sums rounded to
+            // float: relative error below 2e-7, far inside the fit's tolerance; FP64
+            // is slow on this part and only the optional pedestal output needs it)
+            const float ped = MODE == kModeReal ? 0.f : (float)sums[2 * w] * (float)sums[2 * w + 1];
             const int j = lane < 6 ? lane : 0;
             // numerator / denominator positions of lane j's logarithm
             const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
@@ -817,7 +819,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds) p.peds[gw] = ped64;
+                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sums[2 * w] * (double)sums[2 * w + 1];
             }
         }
         tcx::fence_before();

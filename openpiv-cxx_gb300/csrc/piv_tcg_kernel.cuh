@@ -517,8 +517,10 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
                 t1 = n1;
             }
             if (lane == 0) {
-                const double ped64 = real ? 0.0 : (double)sums[2 * wi] * (double)sums[2 * wi + 1];
-                const float ped = (float)ped64;
+                // the pedestal for the fit in FP32 (the exact integer sums rounded to
+                // float: relative error below 2e-7, far inside the fit's tolerance; FP64
+                // is slow on this part and only the optional pedestal output needs it)
+                const float ped = real ? 0.f : (float)sums[2 * wi] * (float)sums[2 * wi + 1];
                 opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
                 int32_t code = -1;
                 const bool has2 = t1 > TC_NEG_INF;
@@ -551,7 +553,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds) p.peds[gw] = ped64;
+                if (p.peds) p.peds[gw] = real ? 0.0 : (double)sums[2 * wi] * (double)sums[2 * wi + 1];
             }
         }
         tcx::fence_before();
