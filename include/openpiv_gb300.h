@@ -220,11 +220,13 @@ int opiv_plan_set_plane_output(opiv_plan* plan, float* d_planes, double* d_pedes
 
 /* ---- adjoint: d(u, v) / d(pixels) --------------------------------------------
  * No counterpart in the reference.  For a pair and the peak codes of a
- * pass over it (the d_out_peak of opiv_process_pair_device; complex or
- * pocket modes, single-pass plans), the vector u = W/2 - px - fx,
+ * pass over it (the d_out_peak of opiv_process_pair_device; any
+ * correlation mode, single-pass plans), the vector u = W/2 - px - fx,
  * v = W/2 - py - fy depends on the pixels only through the 3-point fit of
- * five plane values, each a direct correlation sum; the adjoint recomputes
- * them (no plane is stored) and
+ * five plane values, each a direct correlation sum (REAL mode: of the
+ * windows with each row's mean and each column's mean and alternating
+ * mean removed, which is what its zeroed spectrum column 0 and rows 0,
+ * H/2 amount to); the adjoint recomputes them (no plane is stored) and
  *  - with d_cotangent (n_win x 2 floats: dL/du, dL/dv per window) adds the
  *    vector-Jacobian product into d_grad_a / d_grad_b (float images of the
  *    frames' size, grad_pitch_bytes per row; accumulated, not cleared);

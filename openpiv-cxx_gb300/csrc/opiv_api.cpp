@@ -1652,8 +1652,6 @@ int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_
     if (d_cotangent && (grad_pitch_bytes % sizeof(float) != 0 ||
                         grad_pitch_bytes < sizeof(float) * plan->img_w))
         return fail(OPIV_ERR_ARG, "gradient pitch %zu too small or not a multiple of 4", grad_pitch_bytes);
-    if (plan->mode != OPIV_CORR_COMPLEX)
-        return fail(OPIV_ERR_UNSUPPORTED, "the adjoint covers the complex-type modes");
     if (!is_pow2(plan->ia))
         return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", plan->ia, plan->ia);
     if (pitch_bytes < (size_t)plan->img_w * px_bytes(plan->dtype) ||
@@ -1666,7 +1664,7 @@ int opiv_plan_adjoint(opiv_plan* plan, const void* d_fa, const void* d_fb, size_
     k.fa = d_fa;
     k.fb = d_fb;
     k.pitch = pitch_bytes;
-    const cudaError_t e = launch_piv_adjoint(k, (int)plan->ia, plan->dtype, d_peak, d_cotangent,
+    const cudaError_t e = launch_piv_adjoint(k, (int)plan->ia, plan->dtype, plan->mode, d_peak, d_cotangent,
                                              d_grad_a, d_grad_b, grad_pitch_bytes / sizeof(float),
                                              var_a, var_b, d_sigma, (cudaStream_t)stream);
     cudaSetDevice(prev);

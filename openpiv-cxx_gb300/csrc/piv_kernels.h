@@ -61,11 +61,11 @@ enum { kTcG1 = 0, kTcNS = 1, kTcC = 2, kTcS = 3, kTcC4 = 4, kTcNumMat = 5 };
 bool tc_supports(int w, int dtype);
 size_t tc_constant_bytes(int w);
 void tc_constants(int w, unsigned char* out);
-// Adjoint of a pass (piv_adjoint.cu): complex-mode planes, peaks from the
-// forward pass, cotangents (n_win x 2) pulled back into float image
+// Adjoint of a pass (piv_adjoint.cu): complex or REAL mode planes, peaks
+// from the forward pass, cotangents (n_win x 2) pulled back into float image
 // gradients (accumulated, gpitch floats per row) and/or the propagated
 // standard deviation of u, v (n_win x 2) for pixel noise variances var_a, var_b.
-cudaError_t launch_piv_adjoint(const PivParams& p, int w, int dtype, const int32_t* peaks,
+cudaError_t launch_piv_adjoint(const PivParams& p, int w, int dtype, int mode, const int32_t* peaks,
                                const float* cot, float* grad_a, float* grad_b, size_t gpitch,
                                float var_a, float var_b, float* sigma, cudaStream_t s);
 

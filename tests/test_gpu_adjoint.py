@@ -15,11 +15,11 @@ def _torch():
     return pytest.importorskip("torch")
 
 
-def forward(a, b, step):
+def forward(a, b, step, mode=og.CORR_COMPLEX):
     """Vectors and peak codes of the exact-parity path, device copies kept."""
     torch = _torch()
     h, w = a.shape
-    plan = og.Plan(w, h, a.dtype, W, step)
+    plan = og.Plan(w, h, a.dtype, W, step, mode=mode)
     da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
     vec = torch.empty((plan.n, 5), dtype=torch.float32, device="cuda")
     pk = torch.empty(plan.n, dtype=torch.int32, device="cuda")
@@ -188,3 +188,86 @@ def test_propagated_sigma_against_monte_carlo():
     ratio = mc[ok] / pred[ok]
     med = np.median(ratio, axis=0)
     assert np.all(np.abs(med - 1.0) < 0.1), f"median MC / propagated sigma = {med}"
+
+
+# ---- REAL mode (FFT::cross_correlate_real) ------------------------------------
+def project(win):
+    """FP64 window with spectrum column k_x = 0 and rows k_y = 0, H/2 removed:
+    what the reference's partial unpack leaves of it (fft.h:163-183)."""
+    f = np.fft.fft2(win)
+    f[:, 0] = 0
+    f[0, :] = 0
+    f[W // 2, :] = 0
+    return np.fft.ifft2(f).real
+
+
+def test_real_mode_adjoint_against_fp64_gradient():
+    torch = _torch()
+    a, b = synth.config5(size=512)
+    plan, da, db, vec, pk = forward(a, b, 8, og.CORR_REAL)
+    pkn, vecn = pk.cpu().numpy(), vec.cpu().numpy()
+    grid, idx = sampled_windows(plan, 4)
+    f = piv_function(plan)
+    worst, n = 0.0, 0
+    for comp in (0, 1):
+        sel_w = [w for w in idx if pkn[w] >= 0 and np.isfinite(vecn[w, 2 + comp])]
+        ta = torch.from_numpy(a).cuda().requires_grad_(True)
+        tb = torch.from_numpy(b).cuda().requires_grad_(True)
+        uv = f(ta, tb)
+        sel = torch.zeros_like(uv)
+        sel[torch.tensor(sel_w, device="cuda"), comp] = 1.0
+        (uv.nan_to_num() * sel).sum().backward()
+        ga, gb = ta.grad.cpu().numpy(), tb.grad.cpu().numpy()
+        for w in sel_w:
+            x, y = grid[w]
+            ref = reference_gradients(project(a[y:y + W, x:x + W].astype(np.float64)),
+                                      project(b[y:y + W, x:x + W].astype(np.float64)), int(pkn[w]) & 0xFFFF)
+            for got, want in ((ga[y:y + W, x:x + W], ref[2 * comp]), (gb[y:y + W, x:x + W], ref[2 * comp + 1])):
+                scale = np.abs(want).max()
+                if np.isfinite(scale) and scale > 0:
+                    worst = max(worst, np.abs(got - want).max() / scale)
+                    n += 1
+    assert n > 50
+    assert worst < 5e-3, f"REAL-mode adjoint differs from the FP64 gradient by {worst:.2e} of its largest entry"
+
+
+def test_real_mode_adjoint_against_central_differences():
+    """FP64 central differences (h = 1e-3) through the oracle's REAL-mode
+    chain (the reference's cross_correlate_real, peaks, fit)."""
+    from oracle import oracle as O
+    orc = O.get("port")
+    a, b = synth.config5(size=512)
+    plan, da, db, vec, pk = forward(a, b, 8, og.CORR_REAL)
+    pkn, vecn = pk.cpu().numpy(), vec.cpu().numpy()
+    grid, idx = sampled_windows(plan, 4)
+    idx = [w for w in idx if pkn[w] >= 0 and np.isfinite(vecn[w, 2])][:64]
+    torch = _torch()
+    ta = torch.from_numpy(a).cuda().requires_grad_(True)
+    tb = torch.from_numpy(b).cuda()
+    uv = piv_function(plan)(ta, tb)
+    sel = torch.zeros_like(uv)
+    sel[torch.tensor(idx, device="cuda"), 0] = 1.0
+    (uv.nan_to_num() * sel).sum().backward()
+    ga = ta.grad.cpu().numpy()
+    h = 1e-3
+    errs = []
+    for w in idx:
+        x, y = grid[w]
+        wa = a[y:y + W, x:x + W].astype(np.float64)
+        wb = b[y:y + W, x:x + W].astype(np.float64)
+        one = np.array([[0, 0]], np.int32)
+        u0 = orc.process_windows(wa, wb, one, W, og.CORR_REAL)[0]
+        if not np.isfinite(u0[0, 2]):
+            continue
+        g = ga[y:y + W, x:x + W]
+        for flat in np.argsort(-np.abs(g).ravel())[:4]:
+            py, px = divmod(int(flat), W)
+            us = []
+            for sgn in (1, -1):
+                wp = wa.copy()
+                wp[py, px] += sgn * h
+                us.append(orc.process_windows(wp, wb, one, W, og.CORR_REAL)[0][0, 2])
+            fd = (us[0] - us[1]) / (2 * h)
+            errs.append(abs(fd - g[py, px]) / max(abs(fd), 1e-3))
+    assert len(errs) > 40
+    assert np.median(errs) < 1e-3 and np.max(errs) < 5e-2, (np.median(errs), np.max(errs))
