@@ -431,7 +431,41 @@ def run_ours(args):
     if world == 1:
         grid = fp_plan.grid()
         line["cpu_baseline"] = cpu_baseline(a, b, grid)
+        if not args.no_other_workloads:
+            line["other_workloads"] = other_workloads(args)
     print(json.dumps(line), flush=True)
+
+
+def other_workloads(args) -> dict:
+    """Compact records of the other workloads, measured in the same run as
+    the headline (one GPU): the 48-pair multi-pass batch (20 steps), the
+    precision sweep on a 1024^2 crop of the config-2 field (base
+    statistics, every window size and precision), and the adjoint with
+    Monte Carlo over 200 noise seeds (the full workloads: --workload
+    batch / sweep / adjoint)."""
+    import argparse as ap
+
+    t0 = time.perf_counter()
+    b = batch_line(ap.Namespace(steps=20, warmup=3))
+    t1 = time.perf_counter()
+    sw = sweep_line(1024, variants=("base",))
+    t2 = time.perf_counter()
+    adj = adjoint_line(200)
+    t3 = time.perf_counter()
+    keep = ("variant", "ia", "precision", "windows", "kernel_ms", "rms_px", "max_px", "peak_mismatch_rate")
+    return {
+        "batch_48_pairs_64_32_16": {
+            "metric": b["metric"], "value": b["value"], "ms_per_step": b["ms_per_step"],
+            "e2e": b["e2e"]["value"], "e2e_call_ms_streams": b["e2e"]["call_ms_streams"],
+            "schedules": {k: v for k, v in b["schedules"].items() if k != "autotune"},
+            "gpu_launches_per_step": b["gpu_launches"] / b["steps"],
+            "roofline_frac_fp32": b["roofline"]["frac"],
+            "cpu_baseline": b.get("cpu_baseline", {}).get("value"), "seconds": t1 - t0},
+        "precision_sweep_1024": {"rows": [{k: r[k] for k in keep} for r in sw["rows"]],
+                                 "seconds": t2 - t1},
+        "adjoint_2048_f32": {k: adj[k] for k in ("windows", "vjp_ms", "sigma_ms", "fd_check", "monte_carlo")}
+        | {"seconds": t3 - t2},
+    }
 
 
 # ---- batched multi-pass workload ---------------------------------------------------
@@ -493,6 +527,13 @@ def batch_cpu_rate(sizes, frames, budget_s: float = 15.0):
 
 
 def run_batch(args):
+    line = batch_line(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def batch_line(args):
+    """The batched multi-pass workload's JSON line (None on ranks > 0)."""
     rank, world, local = dist_setup(args)
     sizes, frames = batch_frames(seed_offset=BATCH_PAIRS * rank)
     import torch
@@ -618,7 +659,7 @@ def run_batch(args):
     clocks = sampler.stop()
     batch.close()
     if rank != 0:
-        return
+        return None
     peaks = peaks_file()
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -676,7 +717,7 @@ def run_batch(args):
     }
     if world == 1:
         line["cpu_baseline"] = batch_cpu_rate(sizes, frames)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ---- precision sweep -----------------------------------------------------------
@@ -724,6 +765,10 @@ def fp64_numpy_pass(a, b, grid, ia, img_h, chunk=2048):
 
 
 def run_sweep(args):
+    print(json.dumps(sweep_line(args.sweep_size)), flush=True)
+
+
+def sweep_line(size, variants=("base", "sparse", "noisy"), sizes=(16, 32, 48, 64)):
     """Displacement error of every precision against the FP64 reference on
     the config-2 field: windows 16 / 32 / 48 / 64 px at 75 % overlap, at
     config-2 statistics, low seeding (0.005 ppp) and high noise (sigma 80).
@@ -736,14 +781,13 @@ def run_sweep(args):
     from opiv_gb300 import synth
 
     torch.cuda.set_device(0)
-    size = args.sweep_size
     precisions = [("fp32", og.PREC_FP32), ("tc_split_bf16", og.PREC_TC_SPLIT_BF16),
                   ("tc_bf16", og.PREC_TC_BF16), ("tc_split_fp16", og.PREC_TC_SPLIT_FP16),
-                  ("tc_fp16", og.PREC_TC_FP16)]
+                  ("tc_fp16", og.PREC_TC_FP16), ("tc_split2_fp16", og.PREC_TC_SPLIT2_FP16)]
     rows = []
-    for variant in ("base", "sparse", "noisy"):
+    for variant in variants:
         a, b = synth.config4(variant, size)
-        for ia in (16, 32, 48, 64):
+        for ia in sizes:
             step = ia // 4
 
             def plan(prec):
@@ -759,8 +803,8 @@ def run_sweep(args):
             else:
                 ref_vec, ref_pk = plan(og.PREC_FP64).process(a, b)
             for name, prec in precisions:
-                if prec == og.PREC_FP32 and ia == 48:
-                    continue
+                if (prec == og.PREC_FP32 and ia == 48) or (prec == og.PREC_TC_SPLIT2_FP16 and ia != 32):
+                    continue   # the FFT path takes powers of 2; the two-MMA split 32 px windows
                 p = plan(prec)
                 vec, pk = p.process(a, b)
                 p.set_timing(True)
@@ -770,13 +814,16 @@ def run_sweep(args):
                 rows.append({"variant": variant, "ia": ia, "step": step, "precision": name,
                              "windows": p.n, "kernel_ms": ms,
                              **accuracy(vec, pk, ref_vec, ref_pk)})
-    print(json.dumps({"metric": "precision sweep vs FP64 reference", "size": size,
-                      "data": "synthetic config-2 field (seeded particle images, 12-bit)",
-                      "rows": rows}), flush=True)
+    return {"metric": "precision sweep vs FP64 reference", "size": size,
+            "data": "synthetic config-2 field (seeded particle images, 12-bit)", "rows": rows}
 
 
 # ---- adjoint and uncertainty ------------------------------------------------------
 def run_adjoint(args):
+    print(json.dumps(adjoint_line(args.mc_seeds)), flush=True)
+
+
+def adjoint_line(mc_seeds):
     """The config-5 workload: a 2048^2 float32 pair (0.02 ppp, shift (0.40,
     0.25), noise sigma 0.02), 32 px windows at step 16 (16,129 windows).
     The adjoint of every vector against FP64 central differences through
@@ -858,7 +905,7 @@ def run_adjoint(args):
     same = torch.ones(plan.n, dtype=torch.bool, device="cuda")
     dpk = torch.empty_like(pk)
     pk0d = pk.clone()
-    seeds = args.mc_seeds
+    seeds = mc_seeds
     for _ in range(seeds):
         na = c0a + sig * torch.randn(c0a.shape, generator=gen, device="cuda")
         nb = c0b + sig * torch.randn(c0b.shape, generator=gen, device="cuda")
@@ -872,7 +919,7 @@ def run_adjoint(args):
     ok = same.cpu().numpy() & (pk0 >= 0) & np.isfinite(pred).all(1) & (pred > 0).all(1) & np.isfinite(mc).all(1)
     ratio = mc[ok] / pred[ok]
     q = np.percentile(ratio, [25, 50, 75], axis=0)
-    print(json.dumps({
+    return {
         "metric": "adjoint and propagated uncertainty", "workload": "config5_2048sq_f32_ia32_step16",
         "windows": plan.n, "vjp_ms": vjp_ms, "sigma_ms": sigma_ms,
         "fd_check": {"windows": int(len(sample)), "pixels": int(len(errs)), "h": h,
@@ -883,7 +930,7 @@ def run_adjoint(args):
                         "ratio_mc_over_propagated_v": {"p25": q[0, 1], "median": q[1, 1], "p75": q[2, 1]},
                         "median_sigma_u_px": float(np.median(pred[ok, 0])),
                         "median_sigma_v_px": float(np.median(pred[ok, 1]))},
-        "data": "synthetic (seeded float32 particle images, config 5)"}), flush=True)
+        "data": "synthetic (seeded float32 particle images, config 5)"}
 
 
 def run_reference(args):
@@ -956,6 +1003,8 @@ def main():
     ap.add_argument("--mc-seeds", type=int, default=1000, help="Monte Carlo seeds of the adjoint workload")
     ap.add_argument("--sweep-size", type=int, default=2048,
                     help="image size of the precision sweep")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="pair workload: skip the compact batch / sweep / adjoint records")
     ap.add_argument("--reference-seconds", type=float, default=120.0,
                     help="CPU seconds of the reference arm's warm-up plus timed steps")
     args = ap.parse_args()
