@@ -161,12 +161,18 @@ def test_full_range_uint16(ia, step):
         assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH, (precision, rms, mx, mm)
 
 
-def test_limited_search_and_u8():
+@pytest.mark.parametrize("step", [16, 8])
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_limited_search_and_u8(step, mode):
+    """8-bit frames with the limited search; step 16 runs row tiles (the
+    plain form), step 8 vertical tiles (the grouped form); both modes."""
     a, b = synth.config1()
-    ref = run(a, b, 16, og.PREC_FP64, limit=True)
-    got = run(a, b, 16, og.PREC_TC_SPLIT_BF16, limit=True)
-    rms, mx, mm = displacement_error(got, ref)
-    assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH
+    ref = run(a, b, step, og.PREC_FP64, mode=mode, limit=True)
+    for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16):
+        got = run(a, b, step, precision, mode=mode, limit=True)
+        rms, mx, mm = displacement_error(got, ref)
+        rms_t, max_t, mm_t = BOUNDS[precision]
+        assert rms <= rms_t and mx <= max_t and mm <= mm_t, (step, mode, precision, rms, mx, mm)
 
 
 def test_fp64_pass_equals_certified_fp32_path():
