@@ -336,8 +336,8 @@ std::vector<core::image_view<ContainedT>> find_peaks(const ImageT<ContainedT>& i
     std::vector<double> plane((size_t)W * H);
     detail::to_real(im, plane.data());
     // the host helper of the C ABI: the peaks of one plane the caller holds
-    std::vector<int32_t> xy(2 * (size_t)(W * H) + 2);
-    std::vector<double> values((size_t)(W * H) + 1);
+    std::vector<int32_t> xy(2 * (size_t)num_peaks + 2);
+    std::vector<double> values((size_t)num_peaks + 1);
     const int n = opiv_find_peaks(plane.data(), W, H, num_peaks, peak_radius, xy.data(), values.data());
     detail::check(n);
     std::vector<core::image_view<ContainedT>> result;
