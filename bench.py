@@ -803,8 +803,8 @@ def sweep_line(size, variants=("base", "sparse", "noisy"), sizes=(16, 32, 48, 64
             else:
                 ref_vec, ref_pk = plan(og.PREC_FP64).process(a, b)
             for name, prec in precisions:
-                if (prec == og.PREC_FP32 and ia == 48) or (prec == og.PREC_TC_SPLIT2_FP16 and ia != 32):
-                    continue   # the FFT path takes powers of 2; the two-MMA split 32 px windows
+                if prec == og.PREC_FP32 and ia == 48:
+                    continue   # the FFT path takes powers of 2
                 p = plan(prec)
                 vec, pk = p.process(a, b)
                 p.set_timing(True)

@@ -158,7 +158,7 @@ int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
  * OPIV_PREC_TC_SPLIT_FP16 / OPIV_PREC_TC_FP16: the same with FP16 operands
  *   (11-bit significand), kept inside FP16's range by powers of two (a
  *   fixed one per stage, one per window for the product), undone exactly.
- * OPIV_PREC_TC_SPLIT2_FP16: 32 px windows; FP16 operands with the data
+ * OPIV_PREC_TC_SPLIT2_FP16: FP16 operands with the data
  *   split into hi + lo and the constant matrices single FP16 (hi*C + lo*C,
  *   two MMAs per product instead of three): the data carries ~22 bits, the
  *   DFT constants 11, so the error is set by the constants' rounding.

@@ -1684,8 +1684,6 @@ int opiv_plan_set_precision(opiv_plan* plan, int precision)
         if (!tc_supports((int)plan->ia, plan->dtype))
             return fail(OPIV_ERR_UNSUPPORTED,
                         "the tensor-core path takes 16, 32, 48 or 64 px windows of u8/u16 frames");
-        if (precision == OPIV_PREC_TC_SPLIT2_FP16 && plan->ia != 32)
-            return fail(OPIV_ERR_UNSUPPORTED, "the two-MMA split precision takes 32 px windows");
         if (plan->ia == 32 && (plan->g.xs % 8 != 0 || plan->dx % 8 != 0))
             return fail(OPIV_ERR_UNSUPPORTED,
                         "the 32 px tensor-core path needs window x positions on multiples of 8 pixels");

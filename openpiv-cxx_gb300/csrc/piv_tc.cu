@@ -17,11 +17,11 @@ cudaError_t launch_piv_tc_fp16(const PivParams& p, int dtype, int mode, int limi
                                const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tc_fp16x2(const PivParams& p, int dtype, int mode, int limit, const void* consts,
                                  cudaStream_t s);
-cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s);
-cudaError_t launch_piv_tcg_w48(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+cudaError_t launch_piv_tcg_w48(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s);
-cudaError_t launch_piv_tcg_w64(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+cudaError_t launch_piv_tcg_w64(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s);
 
 namespace tc {
@@ -148,17 +148,15 @@ cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int li
 {
     const unsigned char* c = static_cast<const unsigned char*>(consts);
     const unsigned char* set = c + (fp16 ? tc::set_bytes(w) : 0);
-    if (passes == 2) {   // data split, constants single: FP16, 32 px windows
-        if (w != 32 || !fp16) return cudaErrorInvalidValue;
-        return launch_piv_tc_fp16x2(p, dtype, mode, limit, set, s);
-    }
+    if (passes == 2 && !fp16) return cudaErrorInvalidValue;   // data split: FP16 operands
+    if (passes == 2 && w == 32) return launch_piv_tc_fp16x2(p, dtype, mode, limit, set, s);
     const bool split = passes == 3;
     switch (w) {
-    case 16: return launch_piv_tcg_w16(p, dtype, mode, limit, split, fp16, set, s);
+    case 16: return launch_piv_tcg_w16(p, dtype, mode, limit, passes, fp16, set, s);
     case 32: return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, set, s)
                          : launch_piv_tc_bf16(p, dtype, mode, limit, split, set, s);
-    case 48: return launch_piv_tcg_w48(p, dtype, mode, limit, split, fp16, set, s);
-    case 64: return launch_piv_tcg_w64(p, dtype, mode, limit, split, fp16, set, s);
+    case 48: return launch_piv_tcg_w48(p, dtype, mode, limit, passes, fp16, set, s);
+    case 64: return launch_piv_tcg_w64(p, dtype, mode, limit, passes, fp16, set, s);
     default: return cudaErrorInvalidValue;
     }
 }

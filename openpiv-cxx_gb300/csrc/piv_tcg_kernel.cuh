@@ -51,7 +51,8 @@ using tc::widen8;
 
 constexpr int kThreads = 128;
 
-template <int W, bool SPLIT>
+// CSPLIT: the constants' lo parts are used (and held in shared memory)
+template <int W, bool SPLIT, bool CSPLIT = SPLIT>
 struct Geo {
     static constexpr int H = W / 2;
     static constexpr int WPM = W <= 64 && 64 % W == 0 ? 64 / W : 1;   // windows per stage-1 M tile
@@ -62,7 +63,8 @@ struct Geo {
     static constexpr int KS = W / 16;         // 16-deep MMA steps over a W-long K
     static constexpr int kMat = W * W * 2;    // one W x W 16-bit matrix, K-major
     static constexpr int kSet = kTcNumMat * kMat;
-    static constexpr int kParts = SPLIT ? 2 : 1;
+    static constexpr int kParts = SPLIT ? 2 : 1;          // data operand parts
+    static constexpr int kCParts = CSPLIT ? 2 : 1;        // constant parts
     static constexpr int kOp = 512 * W;       // largest operand (hi part), bytes
     static constexpr int PS = W + 1;          // plane row stride (floats)
     static constexpr int XS = 2 * W + 1;      // exchange row stride (floats), odd
@@ -70,7 +72,7 @@ struct Geo {
     static constexpr int kPlane = 4 * R2 * PS;
     static constexpr int kScratch = ((kXch > kPlane ? kXch : kPlane) + 127) / 128 * 128;
     static constexpr int kTail = 256;
-    static constexpr int kSmem = kParts * kSet + kParts * kOp + kScratch + kTail;
+    static constexpr int kSmem = kCParts * kSet + kParts * kOp + kScratch + kTail;
     static constexpr uint32_t kTmemCols = 2 * W <= 32 ? 32 : (2 * W <= 64 ? 64 : 128);
     static_assert(W % 16 == 0 && W >= 16 && W <= 64, "window size");
     static_assert(R1 <= 128 && R2 <= 128 && R3 <= 64, "tile rows");
@@ -90,15 +92,16 @@ __device__ __forceinline__ void put8(unsigned char* base, int off, int lo, const
     }
 }
 
-// D (+)= A * B, split: hi*hi, hi*lo, lo*hi (a, b: descriptors of the hi
-// parts; the lo parts lie alo / blo bytes further)
-template <bool SPLIT>
+// D (+)= A * B, split: hi*hi, hi*lo (CSPLIT: the constant's lo part),
+// lo*hi (a, b: descriptors of the hi parts; the lo parts lie alo / blo
+// bytes further)
+template <bool SPLIT, bool CSPLIT>
 __device__ __forceinline__ void mma3(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, bool acc,
                                      int alo, int blo)
 {
     tcx::mma_bf16(d, a, b, idesc, acc);
     if (SPLIT) {
-        tcx::mma_bf16(d, a, b + (uint64_t)(blo >> 4), idesc, true);
+        if (CSPLIT) tcx::mma_bf16(d, a, b + (uint64_t)(blo >> 4), idesc, true);
         tcx::mma_bf16(d, a + (uint64_t)(alo >> 4), b, idesc, true);
     }
 }
@@ -142,11 +145,11 @@ __device__ __forceinline__ void tld(uint32_t taddr, float* v)
     for (int i = 0; i < N; ++i) tcx::tmem_ld16(taddr + 16 * i, v + 16 * i);
 }
 
-template <int W, bool F16, bool SPLIT, typename PixT>
+template <int W, bool F16, bool SPLIT, bool CSPLIT, typename PixT>
 __global__ void __launch_bounds__(kThreads)
 piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, int limit)
 {
-    using G = Geo<W, SPLIT>;
+    using G = Geo<W, SPLIT, CSPLIT>;
     constexpr int H = G::H, WPM = G::WPM, WPT = G::WPT, KS = G::KS;
     constexpr float kPix = F16 ? 0.0625f : 1.f;
     constexpr float kT = F16 ? 0.015625f : 1.f;
@@ -163,7 +166,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* cst = smem;
-    unsigned char* dat = smem + G::kParts * G::kSet;
+    unsigned char* dat = smem + G::kCParts * G::kSet;
     float* xch = reinterpret_cast<float*>(dat + G::kParts * G::kOp);   // exchange rows, then planes
     // pixel sums [window][frame] as exact integers (row sums are exact FP32
     // accumulator values for integer pixels; window sums reach 2^28)
@@ -186,7 +189,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
     auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
     const int clo = G::kSet, dlo = G::kOp;
 
-    for (int i = tid; i < G::kParts * G::kSet / 16; i += kThreads)
+    for (int i = tid; i < G::kCParts * G::kSet / 16; i += kThreads)
         reinterpret_cast<uint4*>(cst)[i] = consts[i];
     if (tid == 0) {
         tcx::mbar_init(mbar, 1);
@@ -254,7 +257,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             for (int m1 = 0; m1 < 2; ++m1)
 #pragma unroll
                 for (int ks = 0; ks < KS; ++ks)
-                    mma3<SPLIT>(tbase + m1 * W, dK1 + off(m1 * 256 * W + ks * 256), mat(kTcG1, ks), kId1,
+                    mma3<SPLIT, CSPLIT>(tbase + m1 * W, dK1 + off(m1 * 256 * W + ks * 256), mat(kTcG1, ks), kId1,
                                 ks > 0, dlo, clo);
             tcx::commit(mbar);
         }
@@ -292,7 +295,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 2 * KS; ++ks)
-                mma3<SPLIT>(tbase, dMN + off(ks * 4096), ks < KS ? mat(kTcC, ks) : mat(kTcNS, ks - KS), kId2,
+                mma3<SPLIT, CSPLIT>(tbase, dMN + off(ks * 4096), ks < KS ? mat(kTcC, ks) : mat(kTcNS, ks - KS), kId2,
                             ks > 0, dlo, clo);
             tcx::commit(mbar);
         }
@@ -414,7 +417,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 2 * KS; ++ks)
-                mma3<SPLIT>(tbase, dK3 + off(ks * 256), ks < KS ? mat(kTcC, ks) : mat(kTcNS, ks - KS), kId3,
+                mma3<SPLIT, CSPLIT>(tbase, dK3 + off(ks * 256), ks < KS ? mat(kTcC, ks) : mat(kTcNS, ks - KS), kId3,
                             ks > 0, dlo, clo);
             tcx::commit(mbar);
         }
@@ -453,7 +456,7 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < KS; ++ks)
-                mma3<SPLIT>(tbase, dMN + off(ks * 4096), mat(kTcC4, ks), kId4, ks > 0, dlo, clo);
+                mma3<SPLIT, CSPLIT>(tbase, dMN + off(ks * 4096), mat(kTcC4, ks), kId4, ks > 0, dlo, clo);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -565,11 +568,11 @@ piv_tcg_kernel(const PivParams p, const uint4* __restrict__ consts, int mode, in
     if (warp == 0) tcx::tmem_dealloc(tbase, G::kTmemCols);
 }
 
-template <int W, bool F16, bool SPLIT, typename PixT>
+template <int W, bool F16, bool SPLIT, bool CSPLIT, typename PixT>
 cudaError_t launch_t(const PivParams& p, int mode, int limit, const void* consts, cudaStream_t s)
 {
-    using G = Geo<W, SPLIT>;
-    auto kern = piv_tcg_kernel<W, F16, SPLIT, PixT>;
+    using G = Geo<W, SPLIT, CSPLIT>;
+    auto kern = piv_tcg_kernel<W, F16, SPLIT, CSPLIT, PixT>;
     static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
     static std::atomic<int> cap[64];
     int dev = 0;
@@ -611,22 +614,26 @@ cudaError_t launch_t(const PivParams& p, int mode, int limit, const void* consts
     return cudaGetLastError();
 }
 
-// one window size: operand type, split and pixel type
+// one window size: operand type, MMAs per product (3: data and constants
+// split, 2: data split, FP16 only, 1: no split) and pixel type
 template <int W>
-cudaError_t launch_w(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+cudaError_t launch_w(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                      const void* consts, cudaStream_t s)
 {
     const bool u8 = dtype == kU8;
     if (fp16) {
-        if (split) return u8 ? launch_t<W, true, true, uint8_t>(p, mode, limit, consts, s)
-                             : launch_t<W, true, true, uint16_t>(p, mode, limit, consts, s);
-        return u8 ? launch_t<W, true, false, uint8_t>(p, mode, limit, consts, s)
-                  : launch_t<W, true, false, uint16_t>(p, mode, limit, consts, s);
+        if (passes == 3) return u8 ? launch_t<W, true, true, true, uint8_t>(p, mode, limit, consts, s)
+                                   : launch_t<W, true, true, true, uint16_t>(p, mode, limit, consts, s);
+        if (passes == 2) return u8 ? launch_t<W, true, true, false, uint8_t>(p, mode, limit, consts, s)
+                                   : launch_t<W, true, true, false, uint16_t>(p, mode, limit, consts, s);
+        return u8 ? launch_t<W, true, false, false, uint8_t>(p, mode, limit, consts, s)
+                  : launch_t<W, true, false, false, uint16_t>(p, mode, limit, consts, s);
     }
-    if (split) return u8 ? launch_t<W, false, true, uint8_t>(p, mode, limit, consts, s)
-                         : launch_t<W, false, true, uint16_t>(p, mode, limit, consts, s);
-    return u8 ? launch_t<W, false, false, uint8_t>(p, mode, limit, consts, s)
-              : launch_t<W, false, false, uint16_t>(p, mode, limit, consts, s);
+    if (passes == 2) return cudaErrorInvalidValue;
+    if (passes == 3) return u8 ? launch_t<W, false, true, true, uint8_t>(p, mode, limit, consts, s)
+                               : launch_t<W, false, true, true, uint16_t>(p, mode, limit, consts, s);
+    return u8 ? launch_t<W, false, false, false, uint8_t>(p, mode, limit, consts, s)
+              : launch_t<W, false, false, false, uint16_t>(p, mode, limit, consts, s);
 }
 
 }  // namespace tcg

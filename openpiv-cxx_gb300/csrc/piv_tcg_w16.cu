@@ -3,10 +3,10 @@
 
 namespace opiv {
 
-cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, bool split, bool fp16,
+cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s)
 {
-    return tcg::launch_w<16>(p, dtype, mode, limit, split, fp16, consts, s);
+    return tcg::launch_w<16>(p, dtype, mode, limit, passes, fp16, consts, s);
 }
 
 }  // namespace opiv

@@ -192,9 +192,7 @@ def test_precision_argument_errors():
     p16 = og.Plan(260, 256, np.uint16, 16, 8)
     assert p16.grid()[0, 0] == 2
     p16.set_precision(og.PREC_TC_SPLIT_BF16)
-    with pytest.raises(og.OpivError) as e:     # the two-MMA split: 32 px windows only
-        p16.set_precision(og.PREC_TC_SPLIT2_FP16)
-    assert e.value.status == og.ERR_UNSUPPORTED
+    p16.set_precision(og.PREC_TC_SPLIT2_FP16)
     pf = og.Plan(256, 256, np.float32, 32, 8)
     with pytest.raises(og.OpivError) as e:
         pf.set_precision(og.PREC_TC_BF16)
@@ -230,7 +228,8 @@ def test_precision_sweep_variants(variant):
 # ---- 16, 48 and 64 px windows: the generic tensor-core kernel ---------------------
 GENERIC = [(16, 8), (48, 24), (64, 32)]        # window, step on the 1024^2 u8 pair
 GENERIC_PLANE_RTOL = {og.PREC_TC_SPLIT_BF16: 5e-5, og.PREC_TC_BF16: 2e-2,
-                      og.PREC_TC_SPLIT_FP16: 1e-4, og.PREC_TC_FP16: 5e-3}
+                      og.PREC_TC_SPLIT_FP16: 1e-4, og.PREC_TC_FP16: 5e-3,
+                      og.PREC_TC_SPLIT2_FP16: 2e-3}
 
 
 @pytest.mark.parametrize("ia,step", GENERIC)
@@ -240,8 +239,7 @@ def test_generic_planes_match_fp64_fft(ia, step, mode):
     for precision, rtol in GENERIC_PLANE_RTOL.items():
         got = run(a, b, step, precision, mode=mode, planes=True, ia=ia)
         ref, ped = reference_planes(a, b, got["grid"], ia, mode)
-        if precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT_FP16):
-            assert np.array_equal(got["ped"], ped)     # exact: integer sums below 2^24
+        assert np.array_equal(got["ped"], ped)     # exact: integer sums below 2^24
         err = np.abs(got["planes"] - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
         assert err.max() <= rtol, f"{ia} px {precision}: plane error {err.max():.3e} of the plane peak"
 
@@ -255,8 +253,6 @@ def test_generic_vectors_against_fp64(ia, step, orc):
     a, b = synth.config2(size=1024)
     ref = fp64_reference(a, b, step, ia, og.CORR_COMPLEX, orc) if ia == 48 else run(a, b, step, og.PREC_FP64, ia=ia)
     for precision, (rms_t, max_t, mm_t) in BOUNDS.items():
-        if precision == og.PREC_TC_SPLIT2_FP16:   # 32 px windows only
-            continue
         got = run(a, b, step, precision, ia=ia)
         assert np.array_equal(got["grid"], ref["grid"])
         rms, mx, mm = displacement_error(got, ref)
