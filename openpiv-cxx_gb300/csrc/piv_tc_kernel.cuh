@@ -80,6 +80,14 @@ static_assert(kGroups * kGroupCols <= 512, "grouped form: tensor memory");
 constexpr int kLo = 16384;                      // lo-part offset of the operand buffers
 constexpr int kPacked = 8192;                   // E2: k_x-slot-0 rows (after the stage-3 operand)
 constexpr int kPRow = 36;                       // E4 plane row (floats), padded
+// Vertical tiles at a row step of 8: window i's rows start at image row 8 i,
+// the start of core-matrix row group i, so the stage-2 operand is one copy
+// of the tile's 56 image rows that all four windows read.  MN-major, rows
+// (frame, k) in M groups g of 8 (128 bytes apart), image rows in K groups of
+// 8 (kRowGroup = 4 M groups apart), the U and V parts kRowsPart apart:
+// window i's M group 4 i + g at K group j is the image's row group i + j.
+constexpr int kRowGroup = 512;
+constexpr int kRowsPart = 4096;
 // One thread issues every MMA of a stage and commits them to the stage's
 // mbarrier.  The MMAs of the other CTAs on the SM overlap a CTA's waits.
 
@@ -305,6 +313,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     const uint64_t dB = tcx::sdesc(cst_a, 128, 512);
     auto mat = [&](int m, int ks) { return dB + (uint64_t)((m * kMat + ks * 256) >> 4); };
     const uint64_t dA2 = tcx::sdesc(dat_a, 2048, 128);    // MN-major, k-group stride 2 KB
+    const uint64_t dA2s = tcx::sdesc(dat_a, kRowGroup, 128);   // shared image rows (row step 8)
     const uint64_t dA3 = tcx::sdesc(dat_a, 128, 1024);    // K-major, 8 k-groups per row group
     auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
 
@@ -350,6 +359,8 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_after();
     };
 
+    // vertical tiles at row step 8: one shared copy of the image rows
+    const bool rows8 = VT && p.gdy == 8;
     // item mapping of the pixel stage: 8 consecutive lanes fill one core
     // matrix (rows R & 7), so the 16-byte stores are conflict-free
     const int it_r7 = tid & 7, it_g = (tid >> 3) & 3, it_rg = tid >> 5;
@@ -468,9 +479,11 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         wait_mma();
 
         if constexpr (VT) {
-            // ---- E1: each image row's coefficients into every window that
-            // contains it (stage-2 operand, MN-major, rows (window, frame, k)
-            // = 128, K = (U | V) x window row = 64); row sums into rs
+            // ---- E1: each image row's coefficients into the stage-2 operand
+            // (MN-major, rows (window, frame, k) = 128, K = (U | V) x window
+            // row = 64): at row step 8 once, in the rows all windows share,
+            // otherwise into every window that contains the row; row sums
+            // into rs
             float c[32];
             tcx::tmem_ld32(tlane, c);
             const int f = warp >> 1, y = (warp & 1) * 32 + lane;
@@ -482,19 +495,40 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                     if (SPLIT) split8<F16>(c + 8 * q, hi[q], lo[q]);
                     else hi[q] = round8<F16>(c + 8 * q);
                 }
+                if (rows8) {   // once, in M group 2 f + h of row group y / 8
 #pragma unroll
-                for (int i = 0; i < kTile; ++i) {
-                    const int yl = y - i * p.gdy;
-                    if (org[i].x >= 0 && yl >= 0 && yl < W) {
-                        const int g0 = (i * 32 + f * 16) >> 3;
+                    for (int part = 0; part < 2; ++part)
 #pragma unroll
-                        for (int part = 0; part < 2; ++part) {
-                            const int k = part * 32 + yl;
-                            const int base = (k >> 3) * 2048 + (k & 7) * 16;
+                        for (int h = 0; h < 2; ++h) {
+                            const int o = part * kRowsPart + (y >> 3) * kRowGroup + (2 * f + h) * 128 + (y & 7) * 16;
+                            *reinterpret_cast<uint4*>(dat + o) = hi[2 * part + h];
+                            if (SPLIT) *reinterpret_cast<uint4*>(dat + kLo + o) = lo[2 * part + h];
+                        }
+                } else {
 #pragma unroll
-                            for (int h = 0; h < 2; ++h) {
-                                *reinterpret_cast<uint4*>(dat + base + (g0 + h) * 128) = hi[2 * part + h];
-                                if (SPLIT) *reinterpret_cast<uint4*>(dat + kLo + base + (g0 + h) * 128) = lo[2 * part + h];
+                    for (int i = 0; i < kTile; ++i) {
+                        const int yl = y - i * p.gdy;
+                        if (org[i].x >= 0 && yl >= 0 && yl < W) {
+                            const int g0 = (i * 32 + f * 16) >> 3;
+                            // frame B: the row sign (-1)^y of the tile's row
+                            // is (-1)^yl of the window's row times
+                            // (-1)^(i gdy); flip the sign bits where that is -1
+                            const uint32_t neg = (f && ((i * p.gdy) & 1)) ? 0x80008000u : 0u;
+#pragma unroll
+                            for (int part = 0; part < 2; ++part) {
+                                const int k = part * 32 + yl;
+                                const int base = (k >> 3) * 2048 + (k & 7) * 16;
+#pragma unroll
+                                for (int h = 0; h < 2; ++h) {
+                                    uint4 q = hi[2 * part + h];
+                                    q.x ^= neg; q.y ^= neg; q.z ^= neg; q.w ^= neg;
+                                    *reinterpret_cast<uint4*>(dat + base + (g0 + h) * 128) = q;
+                                    if (SPLIT) {
+                                        q = lo[2 * part + h];
+                                        q.x ^= neg; q.y ^= neg; q.z ^= neg; q.w ^= neg;
+                                        *reinterpret_cast<uint4*>(dat + kLo + base + (g0 + h) * 128) = q;
+                                    }
+                                }
                             }
                         }
                     }
@@ -539,9 +573,12 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         if (tid == 0 && !p.mma_skip) {   // N = 64: the U part against [C; S], the V part against [-S; C]
             tcx::fence_after();
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT, CSPLIT>(tbase, dA2 + off(ks * 4096), mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdM64,
-                            ks > 0);
+            for (int ks = 0; ks < 4; ++ks) {
+                // K step ks: part ks / 2, window rows 16 (ks % 2) .. + 15
+                const uint64_t a = rows8 ? dA2s + off((ks >> 1) * kRowsPart + (ks & 1) * 2 * kRowGroup)
+                                         : dA2 + off(ks * 4096);
+                mma3<SPLIT, CSPLIT>(tbase, a, mat(ks < 2 ? kTcC : kTcNS, ks & 1), kIdM64, ks > 0);
+            }
             tcx::commit(mbar);
         }
         wait_mma();

@@ -50,13 +50,13 @@ def reference_planes(a, b, grid, ia=W, mode=og.CORR_COMPLEX):
     return np.fft.fftshift(r, axes=(1, 2)) - ped[:, None, None], ped
 
 
-def run(a, b, step, precision, mode=og.CORR_COMPLEX, limit=False, planes=False, ia=W):
+def run(a, b, step, precision, mode=og.CORR_COMPLEX, limit=False, planes=False, ia=W, dy=None):
     torch = _torch()
     h, w = a.shape
     if ia == 48:   # not a power of 2: a plan of the tensor-core path alone
-        plan = og.Plan(w, h, a.dtype, ia, step, mode=mode, limit_search=limit, tensor_core=precision)
+        plan = og.Plan(w, h, a.dtype, ia, step, dy, mode=mode, limit_search=limit, tensor_core=precision)
     else:
-        plan = og.Plan(w, h, a.dtype, ia, step, mode=mode, limit_search=limit)
+        plan = og.Plan(w, h, a.dtype, ia, step, dy, mode=mode, limit_search=limit)
         plan.set_precision(precision)
     out = {}
     if planes:
@@ -173,6 +173,29 @@ def test_limited_search_and_u8(step, mode):
         rms, mx, mm = displacement_error(got, ref)
         rms_t, max_t, mm_t = BOUNDS[precision]
         assert rms <= rms_t and mx <= max_t and mm <= mm_t, (step, mode, precision, rms, mx, mm)
+
+
+@pytest.mark.parametrize("dy", [3, 4, 8])
+def test_vertical_tiles_row_steps(dy):
+    """Four windows stacked in a grid column at row steps 3, 4 (each image
+    row's coefficients copied into every window containing it) and 8 (one
+    shared copy of the tile's rows, each window reading it from its own
+    row group): planes, exact pedestals and vectors, both split precisions,
+    on a 1024^2 crop whose window count leaves a partial last tile."""
+    a, b = synth.config2(size=1024)
+    a, b = a[:1000, :1000], b[:1000, :1000]
+    ref = run(a, b, 8, og.PREC_FP64, dy=dy)
+    for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16):
+        got = run(a, b, 8, precision, planes=True, dy=dy)
+        assert np.array_equal(got["grid"], ref["grid"])
+        planes, ped = reference_planes(a, b, got["grid"])
+        assert np.array_equal(got["ped"], ped)
+        err = np.abs(got["planes"] - planes).max(axis=(1, 2)) / np.abs(planes).max(axis=(1, 2))
+        rtol = SPLIT_PLANE_RTOL if precision == og.PREC_TC_SPLIT_BF16 else 1e-3
+        assert err.max() <= rtol, (dy, precision, err.max())
+        rms, mx, mm = displacement_error(got, ref)
+        rms_t, max_t, mm_t = BOUNDS[precision]
+        assert rms <= rms_t and mx <= max_t and mm <= mm_t, (dy, precision, rms, mx, mm)
 
 
 def test_fp64_pass_equals_certified_fp32_path():
