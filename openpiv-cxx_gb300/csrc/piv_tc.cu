@@ -17,6 +17,11 @@ cudaError_t launch_piv_tc_fp16(const PivParams& p, int dtype, int mode, int limi
                                const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tc_fp16x2(const PivParams& p, int dtype, int mode, int limit, const void* consts,
                                  cudaStream_t s);
+bool tc16_takes(const PivParams& p);
+cudaError_t launch_piv_tc16_bf16(const PivParams& p, int dtype, int mode, int limit, bool split,
+                                 const void* consts, cudaStream_t s);
+cudaError_t launch_piv_tc16_fp16(const PivParams& p, int dtype, int mode, int limit, int passes,
+                                 const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tcg_w48(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
@@ -152,7 +157,11 @@ cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int li
     if (passes == 2 && w == 32) return launch_piv_tc_fp16x2(p, dtype, mode, limit, set, s);
     const bool split = passes == 3;
     switch (w) {
-    case 16: return launch_piv_tcg_w16(p, dtype, mode, limit, passes, fp16, set, s);
+    case 16:   // vertical tiles where the grid allows them, else the generic kernel
+        if (tc16_takes(p))
+            return fp16 ? launch_piv_tc16_fp16(p, dtype, mode, limit, passes, set, s)
+                        : launch_piv_tc16_bf16(p, dtype, mode, limit, split, set, s);
+        return launch_piv_tcg_w16(p, dtype, mode, limit, passes, fp16, set, s);
     case 32: return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, set, s)
                          : launch_piv_tc_bf16(p, dtype, mode, limit, split, set, s);
     case 48: return launch_piv_tcg_w48(p, dtype, mode, limit, passes, fp16, set, s);

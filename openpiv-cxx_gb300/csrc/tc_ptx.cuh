@@ -180,6 +180,23 @@ __device__ __forceinline__ void tmem_ld16x2_32(uint32_t taddr, float* v)
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// The same with 16 columns per thread: threads 0-15 columns taddr.col ..
+// +15, threads 16-31 columns taddr.col + 16 .. +31 of lanes taddr.lane + t
+// (half-split offset 16).
+__device__ __forceinline__ void tmem_ld16x2_16(uint32_t taddr, float* v)
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.16x32bx2.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16], 16;\n"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr) : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // max of three floats in one instruction (max.f32 with three sources)
 __device__ __forceinline__ float fmax3(float a, float b, float c)
 {

@@ -282,6 +282,50 @@ def test_generic_vectors_against_fp64(ia, step, orc):
         assert rms <= rms_t and mx <= max_t and mm <= mm_t, (ia, precision, rms, mx, mm)
 
 
+# ---- 16 px windows on vertical tiles (eight windows stacked in a grid column:
+# row steps 1..6, window x positions on multiples of 4 pixels) ----------------
+@pytest.mark.parametrize("dy", [1, 3, 4, 6])
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_tc16_vertical_tiles_planes(dy, mode):
+    """Planes of every precision against numpy's FP64 correlation, exact
+    pedestals, and every precision's vectors against the FP64 pass, on a 528^2
+    crop of the 8-bit pair (partial last tiles in every grid column)."""
+    a, b = synth.config1()
+    a, b = np.ascontiguousarray(a[:528, :528]), np.ascontiguousarray(b[:528, :528])
+    for precision, rtol in GENERIC_PLANE_RTOL.items():
+        got = run(a, b, 4, precision, mode=mode, planes=True, ia=16, dy=dy)
+        ref, ped = reference_planes(a, b, got["grid"], 16, mode)
+        assert np.array_equal(got["ped"], ped)
+        err = np.abs(got["planes"] - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
+        assert err.max() <= rtol, f"dy {dy} {precision}: plane error {err.max():.3e} of the plane peak"
+    ref = run(a, b, 4, og.PREC_FP64, mode=mode, ia=16, dy=dy)
+    for precision, (rms_t, max_t, mm_t) in BOUNDS.items():
+        got = run(a, b, 4, precision, mode=mode, ia=16, dy=dy)
+        assert np.array_equal(got["grid"], ref["grid"])
+        rms, mx, mm = displacement_error(got, ref)
+        assert rms <= rms_t and mx <= max_t and mm <= mm_t, (dy, precision, rms, mx, mm)
+
+
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_tc16_limited_search_u16(mode):
+    """The limited peak search on 16-bit frames (config-2 statistics), and a
+    grid whose x positions are not multiples of 4 (the generic kernel).
+    On 16 px windows with the 8 px search area a few windows have an
+    ill-conditioned fit, which the operands' rounding moves by up to ~5e-3 px
+    (split BF16) and ~3e-2 px (two-MMA split, single FP16 constants), both
+    kernels alike: the largest errors are held to 1e-2 and 5e-2 px here, the
+    RMS to the usual bounds."""
+    a, b = synth.config2(size=1024)
+    bounds = {og.PREC_TC_SPLIT_BF16: (SPLIT_RMS, 1e-2, SPLIT_MISMATCH),
+              og.PREC_TC_SPLIT2_FP16: (SPLIT2_RMS, 5e-2, SPLIT2_MISMATCH)}
+    for dx, dy in ((4, 4), (6, 4)):
+        ref = run(a, b, dx, og.PREC_FP64, mode=mode, limit=True, ia=16, dy=dy)
+        for precision, (rms_t, max_t, mm_t) in bounds.items():
+            got = run(a, b, dx, precision, mode=mode, limit=True, ia=16, dy=dy)
+            rms, mx, mm = displacement_error(got, ref)
+            assert rms <= rms_t and mx <= max_t and mm <= mm_t, (dx, dy, precision, rms, mx, mm)
+
+
 def test_generic_limited_search_and_errors():
     a, b = synth.config1()
     for ia, step in GENERIC:
