@@ -62,8 +62,10 @@ constexpr int kSet = kTcNumMat * kMat;
 constexpr int kDataBytes = 16384;               // stage-2 operand, hi and lo (its largest user)
 constexpr int kLo = 8192;                       // lo-part offset of the operand buffers
 constexpr int kPacked = 4096;                   // E2: k_x-slot-0 rows (after the stage-3 operand)
+constexpr int kPkWin = 80;                      // E2: floats per window there (the two windows of
+                                                // a warp 16 banks apart)
 constexpr int kPRow = 20;                       // E4 plane row (floats), padded to 16 bytes
-constexpr int kTailBytes = 1024;                // sums, origins, indices, row sums, mbarrier, slots
+constexpr int kTailBytes = 1024;                // origins, indices, row sums, mbarrier, slots
 constexpr int kGroupBytes = kDataBytes + kTailBytes;
 constexpr uint32_t kGroupCols = 32;
 constexpr uint32_t kA1 = 16;                    // TMEM column of the stage-1 operand (hi, then lo)
@@ -175,12 +177,11 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
     unsigned char* cst = smem;
     const int grp = (int)(threadIdx.x / kThreads);
     unsigned char* dat = smem + S::kConstBytes + grp * kGroupBytes;
-    // pixel sums [window][frame] (exact integers: a row sum is an exact
-    // FP32 accumulator value, at most 2^20 for 16 16-bit pixels)
-    int* sums = reinterpret_cast<int*>(dat + kDataBytes);
-    int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // this tile's, then the next tile's
+    int2* org = reinterpret_cast<int2*>(dat + kDataBytes);              // this tile's, then the next tile's
     int* gwi = reinterpret_cast<int*>(org + 2 * kTile);
-    float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);              // row sums [frame][row]
+    // row sums [frame][row] (exact integers: a row sum is an exact FP32
+    // accumulator value, at most 2^20 for 16 16-bit pixels)
+    float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);
     int* escale = reinterpret_cast<int*>(rs + 128);                     // F16: product exponent per window
     uint64_t* mbar = reinterpret_cast<uint64_t*>(escale + kTile);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
@@ -346,14 +347,6 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_proxy();
         tcx::fence_before();
         gsync();
-        if (tid >= 32 && tid < 32 + 2 * kTile) {   // window sums from the row sums
-            const int i = (tid - 32) >> 1, f = tid & 1;
-            int s = 0;
-            if (org[i].x >= 0)
-#pragma unroll 4
-                for (int yl = 0; yl < W; ++yl) s += __float2int_rn(rs[f * 64 + i * p.gdy + yl] * kSumUnscale);
-            sums[2 * i + f] = s;
-        }
 
         // ---- stage 2: conj of the column DFT (N = 32): the U part against
         // [C; S], the V part against [-S; C]
@@ -374,7 +367,7 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
             float x[32];   // [k_y] = Re X, [16 + k_y] = -Im X of this lane's (frame, k_x)
             tcx::tmem_ld32(tlane, x);
             // k_x slot 0 rows of both frames for the packed bins
-            float* pk = reinterpret_cast<float*>(dat + kPacked) + wi * 64;
+            float* pk = reinterpret_cast<float*>(dat + kPacked) + wi * kPkWin;
             if (kxr == 0) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
@@ -577,7 +570,16 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
                         make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
             }
             __syncwarp();
-            const float ped = MODE == kModeReal ? 0.f : (float)sums[2 * wi] * (float)sums[2 * wi + 1];
+            // the window's pixel sums from the row sums (lane y: row y of both
+            // frames, added over the 16 lanes of the half)
+            int sum_a = __float2int_rn(rs[wi * p.gdy + y] * kSumUnscale);
+            int sum_b = __float2int_rn(rs[64 + wi * p.gdy + y] * kSumUnscale);
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) {
+                sum_a += __shfl_xor_sync(0xffffffffu, sum_a, o);
+                sum_b += __shfl_xor_sync(0xffffffffu, sum_b, o);
+            }
+            const float ped = MODE == kModeReal ? 0.f : (float)sum_a * (float)sum_b;
             const int j = y < 6 ? y : 0;
             const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
             const int ny = (j == 3 || j == 4) ? py - 1 : (j == 5 ? py + 1 : py);
@@ -619,7 +621,7 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sums[2 * wi] * (double)sums[2 * wi + 1];
+                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sum_a * (double)sum_b;
             }
         }
         tcx::fence_before();

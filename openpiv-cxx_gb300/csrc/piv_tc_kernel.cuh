@@ -560,13 +560,6 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_proxy();
         tcx::fence_before();
         gsync();
-        if (VT && tid >= 32 && tid < 32 + 2 * kTile) {   // window sums from the row sums
-            const int i = (tid - 32) >> 1, f = tid & 1;
-            int s = 0;
-            if (org[i].x >= 0)
-                for (int yl = 0; yl < W; ++yl) s += __float2int_rn(rs[f * 64 + i * p.gdy + yl] * kSumUnscale);
-            sums[2 * i + f] = s;
-        }
 
         // ---- stage 2: conj of the column DFT: Re = U*C + V*(-S),
         // -Im = U*S + V*C
@@ -809,12 +802,27 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                         make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
             }
             __syncwarp();
+            // the window's pixel sums: vertical tiles add their row sums here
+            // (lane y: row y of both frames), row tiles took them in E1
+            int sum_a, sum_b;
+            if constexpr (VT) {
+                sum_a = __float2int_rn(rs[w * p.gdy + y] * kSumUnscale);
+                sum_b = __float2int_rn(rs[64 + w * p.gdy + y] * kSumUnscale);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sum_a += __shfl_xor_sync(0xffffffffu, sum_a, o);
+                    sum_b += __shfl_xor_sync(0xffffffffu, sum_b, o);
+                }
+            } else {
+                sum_a = sums[2 * w];
+                sum_b = sums[2 * w + 1];
+            }
             // REAL mode: the reference's unpack zeroes spectrum row 0, so its
             // plane has no pedestal
             // the pedestal for the fit in FP32 (the exact integer sums rounded to
             // float: relative error below 2e-7, far inside the fit's tolerance; FP64
             // is slow on this part and only the optional pedestal output needs it)
-            const float ped = MODE == kModeReal ? 0.f : (float)sums[2 * w] * (float)sums[2 * w + 1];
+            const float ped = MODE == kModeReal ? 0.f : (float)sum_a * (float)sum_b;
             const int j = lane < 6 ? lane : 0;
             // numerator / denominator positions of lane j's logarithm
             const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
@@ -856,7 +864,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 p.out_vec[gw] = out;
                 if (p.out_peak) p.out_peak[gw] = code;
                 if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sums[2 * w] * (double)sums[2 * w + 1];
+                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sum_a * (double)sum_b;
             }
         }
         tcx::fence_before();
