@@ -65,7 +65,7 @@ constexpr int kPacked = 4096;                   // E2: k_x-slot-0 rows (after th
 constexpr int kPkWin = 80;                      // E2: floats per window there (the two windows of
                                                 // a warp 16 banks apart)
 constexpr int kPRow = 20;                       // E4 plane row (floats), padded to 16 bytes
-constexpr int kTailBytes = 1024;                // origins, indices, row sums, mbarrier, slots
+constexpr int kTailBytes = 1024;                // row sums, exponents, mbarrier, slots
 constexpr int kGroupBytes = kDataBytes + kTailBytes;
 constexpr uint32_t kGroupCols = 32;
 constexpr uint32_t kA1 = 16;                    // TMEM column of the stage-1 operand (hi, then lo)
@@ -177,11 +177,9 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
     unsigned char* cst = smem;
     const int grp = (int)(threadIdx.x / kThreads);
     unsigned char* dat = smem + S::kConstBytes + grp * kGroupBytes;
-    int2* org = reinterpret_cast<int2*>(dat + kDataBytes);              // this tile's, then the next tile's
-    int* gwi = reinterpret_cast<int*>(org + 2 * kTile);
     // row sums [frame][row] (exact integers: a row sum is an exact FP32
     // accumulator value, at most 2^20 for 16 16-bit pixels)
-    float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);
+    float* rs = reinterpret_cast<float*>(dat + kDataBytes);
     int* escale = reinterpret_cast<int*>(rs + 128);                     // F16: product exponent per window
     uint64_t* mbar = reinterpret_cast<uint64_t*>(escale + kTile);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
@@ -238,21 +236,31 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_after();
     };
 
-    for (int tile = t_begin; tile < t_end; ++tile) {
-        if (tid < 2 * kTile) {   // this tile's windows, then the next tile's; x < 0: no window
-            const int t = tile + (tid >> 3), i = tid & (kTile - 1);
-            const int col = t / per_line, row = kTile * (t - col * per_line) + i;
-            const bool ok = t < t_end && col < p.gnx && row < gny;
-            org[tid] = ok ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy) : make_int2(-1, -1);
-            gwi[tid] = row * p.gnx + col;
-        }
-        gsync();
+    // the tile's position, kept in registers by every thread: grid column
+    // lc, first row lr (tile t: column t / per_line, rows kTile * (t %
+    // per_line) + i)
+    int lc = t_begin / per_line;
+    int lr = kTile * (t_begin - lc * per_line);
+    auto advance = [&](int& c, int& r) {
+        r += kTile;
+        if (r >= per_line * kTile) { r = 0; ++c; }
+    };
+    // window i of tile t at (c, r): its corner (x < 0: no window) and grid index
+    auto window = [&](int t, int c, int r, int i, int& gi) {
+        const int row = r + i;
+        gi = row * p.gnx + c;
+        return (t < t_end && c < p.gnx && row < gny) ? make_int2(p.gx0 + c * p.gdx, p.gy0 + row * p.gdy)
+                                                     : make_int2(-1, -1);
+    };
+
+    for (int tile = t_begin; tile < t_end; ++tile, advance(lc, lr)) {
+        int nc = lc, nr = lr;
+        advance(nc, nr);
+        auto org = [&](int i) { int gi; return window(tile, lc, lr, i, gi); };
 
         // image rows of this tile below its top (windows 0 .. nv - 1)
-        int nv = 0;
-#pragma unroll
-        for (int i = 0; i < kTile; ++i) nv += org[i].x >= 0 ? 1 : 0;
-        const int vrows = nv > 0 ? (nv - 1) * p.gdy + W : 0;
+        const int nv = gny - lr < kTile ? gny - lr : kTile;
+        const int vrows = (nv - 1) * p.gdy + W;
 
         // ---- stage-1 operand in tensor memory: thread tid owns lane tid =
         // row R = f * 64 + y.  A row's 16 pixels, widened (frame B rows
@@ -261,7 +269,8 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
         {
             const int f = tid >> 6, y = tid & 63;
             const PixT* row = nullptr;
-            if (y < vrows) row = (f ? fb : fa) + (size_t)(org[0].y + y) * pitch + org[0].x;
+            const int2 o = org(0);
+            if (y < vrows) row = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x;
             typename Raw<PixT>::type raw[2] = { Raw<PixT>::zero(), Raw<PixT>::zero() };
             if (row) load16<PixT>(row, raw);
             const float sg = ((f && (y & 1)) ? -1.f : 1.f) * kPix;
@@ -296,7 +305,8 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         // the next tile's window rows into L2 while this tile computes
         {
-            const int2 o = org[kTile];
+            int gi;
+            const int2 o = window(tile + 1, nc, nr, 0, gi);
             const int f = tid >> 6, y = tid & 63;
             if (o.x >= 0 && y < 7 * kMaxStep + W && o.y + y < p.img_h) {
                 const PixT* q = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x;
@@ -324,7 +334,7 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
 #pragma unroll
                 for (int i = 0; i < kTile; ++i) {
                     const int yl = y - i * p.gdy;
-                    if (org[i].x >= 0 && yl >= 0 && yl < W) {
+                    if (i < nv && yl >= 0 && yl < W) {
                         // frame B: (-1)^y of the tile's row is (-1)^yl of the
                         // window's row times (-1)^(i gdy)
                         const uint32_t neg = (f && ((i * p.gdy) & 1)) ? 0x80008000u : 0u;
@@ -505,7 +515,8 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
             const int s = lane >> 4, y = lane & 15;
             const int wi = 2 * warp + s;
             float* pl = reinterpret_cast<float*>(dat) + wi * (W * kPRow);
-            const int gw = gwi[wi];
+            int gw;
+            const int2 ow = window(tile, lc, lr, wi, gw);
             float v[16];
             tcx::tmem_ld16(tlane, v);
             if (F16) {   // undo 2^-26 (pixels, stage-1 matrix, twice), 2^-e (product), 2^-6 (T)
@@ -542,7 +553,7 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
                 }
             const bool row_in = y >= SY0 && y < SY1;
             float t0 = row_in ? T0[0] : TC_NEG_INF, t1 = row_in ? T1[0] : TC_NEG_INF;
-            const bool valid = org[wi].x >= 0;
+            const bool valid = ow.x >= 0;
             if (p.planes && valid) {
 #pragma unroll
                 for (int x = 0; x < W; ++x) p.planes[(size_t)gw * (W * W) + y * W + x] = v[x];
@@ -598,7 +609,7 @@ piv_tc16_kernel(const PivParams p, const uint4* __restrict__ consts)
             if (y == 0 && valid) {
                 opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
                 int32_t code = -1;
-                const int2 o = org[wi];
+                const int2 o = ow;
                 const bool has2 = t1 > TC_NEG_INF;
                 if (has2) {
                     const float vc = pl[py * kPRow + px];

@@ -59,7 +59,7 @@ constexpr int kTile = 4;                        // windows per tile
 constexpr int kMat = 2048;                      // one 32 x 32 BF16 matrix, K-major
 constexpr int kConstBytes = kTcNumMat * 2 * kMat;
 constexpr int kDataBytes = 32 * 1024;   // stage-2 operand, hi and lo parts (its largest user)
-constexpr int kTailBytes = 768;                 // sums, origins, indices, row sums, mbarrier, TMEM slot, flag
+constexpr int kTailBytes = 768;                 // sums, row sums, mbarrier, TMEM slot, flag, exponents
 constexpr int kSmemBytes = kConstBytes + kDataBytes + kTailBytes;
 constexpr uint32_t kTmemCols = 128;
 constexpr uint32_t kA1 = 64;                    // TMEM column of the stage-1 operand (hi, then lo)
@@ -289,9 +289,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     // FP32 accumulator value (integer pixels, at most 2^21 for 32 16-bit
     // pixels); the window sum (up to 2^26) is added in integers
     int* sums = reinterpret_cast<int*>(dat + kDataBytes);
-    int2* org = reinterpret_cast<int2*>(sums + 2 * kTile);              // window corners
-    int* gwi = reinterpret_cast<int*>(org + 2 * kTile);                 // window indices
-    float* rs = reinterpret_cast<float*>(gwi + 2 * kTile);              // VT: row sums [frame][row]
+    float* rs = reinterpret_cast<float*>(sums + 2 * kTile);             // VT: row sums [frame][row]
     uint64_t* mbar = reinterpret_cast<uint64_t*>(rs + 128);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
     int* abort_flag = reinterpret_cast<int*>(tslot + 1);
@@ -365,27 +363,45 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
     // matrix (rows R & 7), so the 16-byte stores are conflict-free
     const int it_r7 = tid & 7, it_g = (tid >> 3) & 3, it_rg = tid >> 5;
 
-    for (int tile = t_begin; tile < t_end; ++tile) {
-        if (tid < 2 * kTile) {   // this tile's windows, then the next tile's; x < 0: no window
-            const int t = tile + (tid >> 2), i = tid & (kTile - 1);
-            int col, row;
-            if (VT) {   // tile t: column t / per_line, rows kTile * (t % per_line) + i
-                const int c = t / per_line;
-                col = c;
-                row = kTile * (t - c * per_line) + i;
-            } else {    // tile t: row t % gny, columns kTile * (t / gny) + i
-                const int c = t / gny;
-                row = t - c * gny;
-                col = kTile * c + i;
-            }
-            const bool ok = t < t_end && col < p.gnx && row < gny;
-            org[tid] = ok ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy) : make_int2(-1, -1);
-            gwi[tid] = row * p.gnx + col;
+    // the tile's position, kept in registers by every thread (a group walks
+    // a contiguous range of tiles): vertical tiles -- grid column lc, first
+    // row lr (tile t: column t / per_line, rows kTile * (t % per_line) + i);
+    // row tiles -- grid row lr, first column lc (tile t: row t % gny,
+    // columns kTile * (t / gny) + i)
+    int lc, lr;
+    if (VT) {
+        lc = t_begin / per_line;
+        lr = kTile * (t_begin - lc * per_line);
+    } else {
+        const int c = t_begin / gny;
+        lr = t_begin - c * gny;
+        lc = kTile * c;
+    }
+    auto advance = [&](int& c, int& r) {
+        if (VT) {
+            r += kTile;
+            if (r >= per_line * kTile) { r = 0; ++c; }
+        } else if (++r >= gny) {
+            r = 0;
+            c += kTile;
         }
-        gsync();
+    };
+    // window i of tile t at (c, r): its corner (x < 0: no window) and grid index
+    auto window = [&](int t, int c, int r, int i, int& gi) {
+        const int col = VT ? c : c + i, row = VT ? r + i : r;
+        gi = row * p.gnx + col;
+        return (t < t_end && col < p.gnx && row < gny) ? make_int2(p.gx0 + col * p.gdx, p.gy0 + row * p.gdy)
+                                                       : make_int2(-1, -1);
+    };
+
+    for (int tile = t_begin; tile < t_end; ++tile, advance(lc, lr)) {
+        int nc = lc, nr = lr;
+        advance(nc, nr);
+        auto org = [&](int i) { int gi; return window(tile, lc, lr, i, gi); };
+        auto org_next = [&](int i) { int gi; return window(tile + 1, nc, nr, i, gi); };
 
         // number of window rows of this tile (VT: image rows below its top)
-        const int vrows = VT ? (org[1].x >= 0 ? (org[2].x >= 0 ? (org[3].x >= 0 ? 3 : 2) : 1) : 0) * p.gdy + W
+        const int vrows = VT ? (org(1).x >= 0 ? (org(2).x >= 0 ? (org(3).x >= 0 ? 3 : 2) : 1) : 0) * p.gdy + W
                              : 0;
         // ---- stage-1 operand in tensor memory: thread tid owns lane tid.
         // VT: row R = tid = f * 64 + y of the tile's image rows (y < vrows);
@@ -404,12 +420,12 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 if constexpr (VT) {
                     f = R >> 6;
                     y = R & 63;
-                    const int2 o = org[0];
+                    const int2 o = org(0);
                     if (o.x >= 0 && y < vrows) row = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x;
                 } else {
                     f = (R >> 5) & 1;
                     y = R & 31;
-                    const int2 o = org[R >> 6];
+                    const int2 o = org(R >> 6);
                     if (o.x >= 0) row = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x;
                 }
                 typename Raw<PixT>::type raw[4];
@@ -454,7 +470,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         // the next tile's window rows into L2 while this tile computes
         if constexpr (VT) {
-            const int2 o = org[kTile];
+            const int2 o = org_next(0);
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 const int R = (it_rg + 4 * t) * 8 + it_r7;
@@ -469,7 +485,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             for (int t = 0; t < 8; ++t) {
                 const int R = (it_rg + 4 * t) * 8 + it_r7;
                 const int w = R >> 6, f = (R >> 5) & 1, y = R & 31;
-                const int2 o = org[kTile + w];
+                const int2 o = org_next(w);
                 if (o.x >= 0) {
                     const PixT* q = (f ? fb : fa) + (size_t)(o.y + y) * pitch + o.x + 8 * it_g;
                     asm volatile("prefetch.global.L2 [%0];" :: "l"(q));
@@ -508,7 +524,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
 #pragma unroll
                     for (int i = 0; i < kTile; ++i) {
                         const int yl = y - i * p.gdy;
-                        if (org[i].x >= 0 && yl >= 0 && yl < W) {
+                        if (org(i).x >= 0 && yl >= 0 && yl < W) {
                             const int g0 = (i * 32 + f * 16) >> 3;
                             // frame B: the row sign (-1)^y of the tile's row
                             // is (-1)^yl of the window's row times
@@ -734,7 +750,8 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
         {
             float* pl = reinterpret_cast<float*>(dat) + warp * (32 * kPRow);
             const int w = warp;
-            const int gw = gwi[w];
+            int gw;
+            const int2 ow = window(tile, lc, lr, w, gw);
             const int y = lane;
             float v[32];
             tcx::tmem_ld32(tlane, v);
@@ -774,7 +791,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             const bool row_in = y >= SY0 && y < SY1;
             float t0 = row_in ? T0[0] : TC_NEG_INF, t1 = row_in ? T1[0] : TC_NEG_INF;
             const int tx = I0[0];
-            const bool valid = org[w].x >= 0;
+            const bool valid = ow.x >= 0;
             if (p.planes && valid) {
 #pragma unroll
                 for (int x = 0; x < W; ++x) p.planes[(size_t)gw * (W * W) + y * W + x] = v[x];
@@ -841,7 +858,7 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
             if (lane == 0 && valid) {
                 opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
                 int32_t code = -1;
-                const int2 o = org[w];
+                const int2 o = ow;
                 const bool has2 = t1 > TC_NEG_INF;
                 if (has2) {
                     const float vc = pl[py * kPRow + px];
