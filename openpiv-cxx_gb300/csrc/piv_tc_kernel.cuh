@@ -884,8 +884,11 @@ piv_tc_kernel(const PivParams p, const uint4* __restrict__ consts)
                 if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sum_a * (double)sum_b;
             }
         }
+        // no group barrier here: the next tile's pixel stage writes only the
+        // stage-1 operand (tensor-memory columns that E4 does not read) in
+        // this warp's own lanes and no shared memory; the barrier after it
+        // orders E4 before the stage-1 MMA and the shared-memory writes
         tcx::fence_before();
-        gsync();
     }
     tcx::fence_before();
     __syncthreads();
