@@ -67,7 +67,7 @@ L2_ROTATION = 4
 # DRAM bytes (read + write) of one launch of the timed kernels on this
 # workload, from ncu captures of the current kernels (the bench cannot
 # profile itself; recaptured whenever a kernel changes)
-TC_TRAFFIC_BYTES = 68_250_880 + 1_459_968
+TC_TRAFFIC_BYTES = 68_225_792 + 1_468_672
 FP32_TRAFFIC_BYTES = 67_200_000 + 3_700_000
 
 
