@@ -39,6 +39,7 @@ independent replicas (one pair each), value is the sum.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -65,10 +66,26 @@ METRIC = "vectors/s"
 WORKLOAD = f"piv_pair_{IMG}x{IMG}_u16_ia{IA}_step{STEP}"
 L2_ROTATION = 4
 # DRAM bytes (read + write) of one launch of the timed kernels on this
-# workload, from ncu captures of the current kernels (the bench cannot
-# profile itself; recaptured whenever a kernel changes)
-TC_TRAFFIC_BYTES = 68_225_792 + 1_468_672
-FP32_TRAFFIC_BYTES = 67_200_000 + 3_700_000
+# workload, from an ncu capture (the bench cannot profile itself), with the
+# SHA-256 prefixes of the kernel sources that capture ran: when a source no
+# longer matches, the line reports no traffic instead of a stale figure
+KERNEL_TRAFFIC = {
+    "tc": {"bytes": 68_225_792 + 1_468_672,
+           "sources": {"piv_tc_kernel.cuh": "52baeb2ef1e34e1b", "tc_ptx.cuh": "4d83992c219d064e"}},
+    "fp32": {"bytes": 67_165_440 + 4_344_832,
+             "sources": {"piv_fp32.cuh": "916731b6afc83819", "fft_reg.cuh": "b328bf1c452ce151"}},
+}
+
+
+def kernel_traffic(kind):
+    """(bytes, source note) of one launch of the tc or fp32 kernel, or
+    (None, why) when its sources changed since the capture."""
+    rec = KERNEL_TRAFFIC[kind]
+    for name, digest in rec["sources"].items():
+        with open(os.path.join(PKG, "csrc", name), "rb") as f:
+            if hashlib.sha256(f.read()).hexdigest()[:16] != digest:
+                return None, f"{name} changed since the ncu capture of its traffic"
+    return rec["bytes"], "dram__bytes_read.sum + dram__bytes_write.sum of one launch, ncu capture of this workload"
 
 
 def peaks_file():
@@ -378,6 +395,7 @@ def run_ours(args):
     achieved = tc_flops / tc_s / 1e12
     value = args.steps * N_WIN * world / tc_el
     plain_value = args.steps * N_WIN * world / fp_el
+    tc_traffic, fp_traffic = kernel_traffic("tc"), kernel_traffic("fp32")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tc_el * 1e3 / args.steps,
@@ -399,10 +417,8 @@ def run_ours(args):
                 "call": "opiv_process_pairs (pinned host frames, copies overlapped with the passes)"},
         "gpu_launches": tc_launches,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                     "frac": achieved / bf16_peak, "traffic": TC_TRAFFIC_BYTES,
-                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                                       "ncu capture of this workload; "
-                                       f"algorithmic bytes {2 * IMG * IMG * 2 + N_WIN * 24}",
+                     "frac": achieved / bf16_peak, "traffic": tc_traffic[0],
+                     "traffic_source": f"{tc_traffic[1]}; algorithmic bytes {2 * IMG * IMG * 2 + N_WIN * 24}",
                      "kernel": "piv_tc_kernel<split,COMPLEX,u16>", "kernel_ms": statistics.mean(tc_ms),
                      "flop": "executed MMA FLOPs: 3 passes x (2 128x32 + 4 128x64 + 4 64x64 + 2 128x32 products, K=16) per 4 windows",
                      "peak_source": "bf16_tflops of MEASURED_PEAKS.json (cuBLAS burst, of measured)",
@@ -417,9 +433,7 @@ def run_ours(args):
             "roofline": {"bound": "fp32", "achieved": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12,
                          "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": FLOP_PER_WINDOW * N_WIN / fp_s / 1e12 / fp32_peak,
-                         "traffic": FP32_TRAFFIC_BYTES,
-                         "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                           "launch, ncu capture of this workload",
+                         "traffic": fp_traffic[0], "traffic_source": fp_traffic[1],
                          "kernel": "piv_fp32_kernel<32,COMPLEX,u16>", "kernel_ms": statistics.mean(fp_ms),
                          "exact_pass_ms": statistics.mean(ex_ms),
                          "flop": "algorithmic: 2 x 5 N log2 N + 8 N, N = 1024, per window",

@@ -9,6 +9,8 @@ time is the slowest rank's and the value the whole job's windows over it.
   single-process run and the aggregate against the ranks' own timings.
 * `python bench.py --gpus 2` outside torchrun launches two ranks itself
   (checked with the reference arm, which runs on CPU).
+* The bench line's DRAM traffic is withheld once the kernel sources differ
+  from those its ncu capture ran.
 """
 import json
 import multiprocessing as mp
@@ -95,3 +97,23 @@ def test_bench_launches_its_ranks(orc, tmp_path):
     lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
     assert len(lines) == 1                               # rank 0 alone prints
     assert lines[0]["impl"] == "reference" and lines[0]["config"]["ranks"] == 2
+
+
+def test_bench_traffic_tracks_kernel_sources(monkeypatch):
+    """The bench line's DRAM traffic comes from an ncu capture of the kernel
+    sources it records (SHA-256 prefixes): reported while they match,
+    withheld (null, with the reason) once a source differs."""
+    import hashlib
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    src = os.path.join(ROOT, "openpiv-cxx_gb300", "csrc", "piv_tc_kernel.cuh")
+    with open(src, "rb") as f:
+        digest = hashlib.sha256(f.read()).hexdigest()[:16]
+    monkeypatch.setitem(bench.KERNEL_TRAFFIC, "tc", {"bytes": 1234, "sources": {"piv_tc_kernel.cuh": digest}})
+    nbytes, note = bench.kernel_traffic("tc")
+    assert nbytes == 1234 and "ncu capture" in note
+    monkeypatch.setitem(bench.KERNEL_TRAFFIC, "tc", {"bytes": 1234, "sources": {"piv_tc_kernel.cuh": "0" * 16}})
+    nbytes, note = bench.kernel_traffic("tc")
+    assert nbytes is None and "piv_tc_kernel.cuh changed" in note
