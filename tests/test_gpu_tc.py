@@ -326,6 +326,21 @@ def test_tc16_limited_search_u16(mode):
             assert rms <= rms_t and mx <= max_t and mm <= mm_t, (dx, dy, precision, rms, mx, mm)
 
 
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_tc16_blank_frames(mode):
+    """Blank frames through the 16 px vertical-tile kernel: every plane is
+    zero, no strict maximum anywhere, so every vector is zero and every peak
+    code -1 (the reference's find_peaks returns fewer than two peaks)."""
+    a = np.zeros((256, 256), np.uint16)
+    for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16, og.PREC_TC_BF16):
+        plan = og.Plan(256, 256, np.uint16, 16, 4, mode=mode)
+        plan.set_precision(precision)
+        vec, pk = plan.process(a, a)
+        plan.status()
+        assert np.all(vec == 0) and np.all(pk == -1), precision
+        plan.close()
+
+
 def test_generic_limited_search_and_errors():
     a, b = synth.config1()
     for ia, step in GENERIC:
