@@ -98,7 +98,8 @@ int64_t opiv_grid_offsets(uint32_t img_w, uint32_t img_h, uint32_t ia_w, uint32_
  * of two (OPIV_ERR_NOT_POW2); other powers of two give OPIV_ERR_UNSUPPORTED.
  * dx, dy: grid step in pixels (generate_cartesian_grid's offsets).
  * limit_search: search peaks only in the centre rect().dilate(0.5) of the
- * plane (main.cpp:204-208). */
+ * plane (main.cpp:204-208).  A grid of more than 2^31 - 1 windows gives
+ * OPIV_ERR_CAPACITY (the kernels index a pass's windows in 32 bits). */
 int opiv_plan_create(opiv_plan** plan, uint32_t img_w, uint32_t img_h, int dtype, uint32_t ia,
                      uint32_t dx, uint32_t dy, int mode, int limit_search, int device);
 int opiv_plan_destroy(opiv_plan* plan);
@@ -383,6 +384,7 @@ int opiv_process_pair_device_noalloc(const void* d_frame_a, const void* d_frame_
  * exact = 0: FP32 kernels + exact pedestal (within 1e-5 of the plane peak);
  * exact = 1: double-precision kernels that repeat the reference's arithmetic
  * operation for operation (bit-identical planes).  Host buffers, synchronous.
+ * At most (2^31 - 1) / w windows per call (OPIV_ERR_CAPACITY beyond).
  * FFT::cross_correlate / cross_correlate_real: fft.h:188-227. */
 int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int64_t n, int mode,
                                int exact, double* out_planes, int device);

@@ -444,6 +444,10 @@ int plan_create(opiv_plan** out, uint32_t img_w, uint32_t img_h, int dtype, uint
     }
     if (g.xs + (int64_t)dx * (g.xc - 1) + ia > (int64_t)img_w || g.ys + (int64_t)dy * (g.yc - 1) + ia > (int64_t)img_h)
         return fail(OPIV_ERR_RECT_OUTSIDE, "extract: rectangle to extract is too large for image");
+    // the kernels index a pass's windows with 32-bit integers
+    if ((int64_t)g.xc * g.yc > (int64_t)INT32_MAX)
+        return fail(OPIV_ERR_CAPACITY, "grid of %lld windows: a plan takes at most 2^31 - 1",
+                    (long long)((int64_t)g.xc * g.yc));
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
@@ -1770,6 +1774,9 @@ int opiv_cross_correlate_batch(const double* a, const double* b, uint32_t w, int
     if (!is_pow2(w)) return fail(OPIV_ERR_NOT_POW2, "dimensions must be power of 2: %ux%u", w, w);
     if (exact ? !exact_supports((int)w) : !fp32_supports((int)w))
         return fail(OPIV_ERR_UNSUPPORTED, "no kernel for %ux%u windows", w, w);
+    // the windows are stacked as rows of one frame, indexed in 32 bits
+    if (n > (int64_t)INT32_MAX / (int64_t)w)
+        return fail(OPIV_ERR_CAPACITY, "%lld windows of %u rows: at most 2^31 - 1 rows in one call", (long long)n, w);
     if (n == 0) return OPIV_OK;
     int prev = 0;
     cudaGetDevice(&prev);

@@ -83,6 +83,13 @@ def test_plan_validation_precedes_device(lib):
     with pytest.raises(og.OpivError) as e:
         og.Plan(100, 100, np.int32, 32, 8)
     assert e.value.status == og.ERR_ARG
+    # 65,521^2 windows: past the 2^31 - 1 a pass indexes (both creators)
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(65536, 65536, np.uint8, 16, 1)
+    assert e.value.status == og.ERR_CAPACITY and "2^31" in e.value.message
+    with pytest.raises(og.OpivError) as e:
+        og.Plan(65536, 65536, np.uint8, 16, 1, tensor_core=og.PREC_TC_SPLIT_BF16)
+    assert e.value.status == og.ERR_CAPACITY
 
 
 def test_tensor_core_plan_validation_precedes_device(lib):
@@ -141,3 +148,15 @@ def test_batch_schedule_calls_check_arguments(lib):
     assert L.opiv_plan_autotune(None, None, None, 0, None) == og.ERR_ARG
     assert L.opiv_plan_test_mma_timeout(None, 1) == og.ERR_ARG
     assert "null" in L.opiv_last_error().decode()
+
+
+def test_batch_correlation_window_limit(lib):
+    """opiv_cross_correlate_batch stacks its windows as the rows of one
+    frame indexed in 32 bits: a count past (2^31 - 1) / w is refused before
+    any buffer or device is touched."""
+    import ctypes as C
+
+    buf = np.zeros(16, np.float64)
+    p = buf.ctypes.data_as(C.POINTER(C.c_double))
+    st = lib.opiv_cross_correlate_batch(p, p, 16, (2 ** 31) // 16 + 1, og.CORR_COMPLEX, 0, p, 0)
+    assert st == og.ERR_CAPACITY
