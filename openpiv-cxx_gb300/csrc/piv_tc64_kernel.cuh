@@ -224,25 +224,24 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
             const int f = tid >> 6, y = tid & 63;
             const PixT* row = (f ? fb : fa) + (size_t)(oy + y) * pitch + ox;
             const float sg = (f && (y & 1)) ? -1.f : 1.f;
-            uint32_t hw[32], lw[32];
 #pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                float px[8];
-                widen8<PixT>(tc::load_raw<PixT>(row + 8 * g), px, sg);
+            for (int hp = 0; hp < 2; ++hp) {   // pixels 32 hp .. 32 hp + 31: columns 16 hp .. + 15
+                uint32_t hw[16], lw[16];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    hw[4 * g + j] = pack2<false>(px[2 * j], px[2 * j + 1]);
-                    if (SPLIT) {
-                        const float2 hf = unpack2<false>(hw[4 * g + j]);
-                        lw[4 * g + j] = pack2<false>(px[2 * j] - hf.x, px[2 * j + 1] - hf.y);
+                for (int g = 0; g < 4; ++g) {
+                    float px[8];
+                    widen8<PixT>(tc::load_raw<PixT>(row + 32 * hp + 8 * g), px, sg);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        hw[4 * g + j] = pack2<false>(px[2 * j], px[2 * j + 1]);
+                        if (SPLIT) {
+                            const float2 hf = unpack2<false>(hw[4 * g + j]);
+                            lw[4 * g + j] = pack2<false>(px[2 * j] - hf.x, px[2 * j + 1] - hf.y);
+                        }
                     }
                 }
-            }
-            tcx::tmem_st16(tlane + kA1, hw);
-            tcx::tmem_st16(tlane + kA1 + 16, hw + 16);
-            if (SPLIT) {
-                tcx::tmem_st16(tlane + kA1 + 32, lw);
-                tcx::tmem_st16(tlane + kA1 + 48, lw + 16);
+                tcx::tmem_st16(tlane + kA1 + 16 * hp, hw);
+                if (SPLIT) tcx::tmem_st16(tlane + kA1 + 32 + 16 * hp, lw);
             }
         }
         tcx::fence_before();
@@ -272,16 +271,16 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         // M = 16 j + 8 f + k % 8 (j = k / 8), K = (U | V) x y; core matrix
         // (K group, M group) at (K / 8) * 1024 + (M / 8) * 128; row sums
         {
-            float c[64];
-            tcx::tmem_ld32x2(tlane, tlane + 32, c, c + 32);
             const int f = tid >> 6, y = tid & 63;
-            rs[f * 64 + y] = (f && (y & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
 #pragma unroll
-            for (int part = 0; part < 2; ++part)
+            for (int part = 0; part < 2; ++part) {   // U (columns 0..31), then V
+                float c[32];
+                tcx::tmem_ld32(tlane + 32 * part, c);
+                if (part == 0) rs[f * 64 + y] = (f && (y & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    put8<SPLIT>(dat, (part * 8 + (y >> 3)) * 1024 + (2 * j + f) * 128 + (y & 7) * 16,
-                                c + part * 32 + 8 * j);
+                    put8<SPLIT>(dat, (part * 8 + (y >> 3)) * 1024 + (2 * j + f) * 128 + (y & 7) * 16, c + 8 * j);
+            }
         }
         tcx::fence_proxy();
         tcx::fence_before();
@@ -304,49 +303,46 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         {
             const int L = lane & 15, hh = lane >> 4;
             const int f = L >> 3, kx = 8 * warp + (L & 7);
-            // [0]: Re at k_y = 16 hh + i, [1]: Re at 32 + 16 hh + i, [2], [3]: -Im
-            float q0[16], q1[16], q2[16], q3[16];
-            tcx::tmem_ld16x2_16(tlane, q0);
-            tcx::tmem_ld16x2_16(tlane + 32, q1);
-            tcx::tmem_ld16x2_16(tlane + 64, q2);
-            tcx::tmem_ld16x2_16(tlane + 96, q3);
             float* pk = reinterpret_cast<float*>(dat + kPacked);   // [frame][Re 64 | -Im 64]
-            if (kx == 0) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int b = f * 128 + 16 * hh + 4 * i;
-                    *reinterpret_cast<float4*>(pk + b) = make_float4(q0[4 * i], q0[4 * i + 1], q0[4 * i + 2], q0[4 * i + 3]);
-                    *reinterpret_cast<float4*>(pk + b + 32) = make_float4(q1[4 * i], q1[4 * i + 1], q1[4 * i + 2], q1[4 * i + 3]);
-                    *reinterpret_cast<float4*>(pk + b + 64) = make_float4(q2[4 * i], q2[4 * i + 1], q2[4 * i + 2], q2[4 * i + 3]);
-                    *reinterpret_cast<float4*>(pk + b + 96) = make_float4(q3[4 * i], q3[4 * i + 1], q3[4 * i + 2], q3[4 * i + 3]);
-                }
-            }
-            // frame a's thread computes k_y = 16 hh + i, frame b's 32 + 16 hh
-            // + i; frame b's columns are rotated by 32, so both find their own
-            // values in q0, q2 and take their partner's (lane ^ 8) q1, q3.
-            // With m = own, o = partner values and n = -Im: Re P = m_r o_r +
-            // m_n o_n, Im P = +-(o_r m_n - o_n m_r), + for frame a.
             const float sq = f ? -1.f : 1.f;
-            float pr[16], pi[16];
+            // frame a's thread computes k_y = 16 hh + 8 h + i, frame b's 32 more
+            // (h: the half, i < 8); frame b's columns are rotated by 32, so
+            // both find their own values in q[i], q[16 + i] (Re, -Im) and take
+            // their partner's (lane ^ 8) q[8 + i], q[24 + i].  With m = own,
+            // o = partner values and n = -Im: Re P = m_r o_r + m_n o_n,
+            // Im P = +-(o_r m_n - o_n m_r), + for frame a.
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const float mr = q0[i], mn = q2[i];
-                const float orr = __shfl_xor_sync(0xffffffffu, q1[i], 8);
-                const float onn = __shfl_xor_sync(0xffffffffu, q3[i], 8);
-                float r = fmaf(mr, orr, mn * onn);
-                float q = sq * fmaf(orr, mn, -(onn * mr));
-                if (i & 1) { r = -r; q = -q; }   // quadrant sign (-1)^k_y
-                if (MODE == kModeReal && i == 0 && hh == 0) { r = 0.f; q = 0.f; }   // k_y = 0 or 32
-                pr[i] = r;
-                pi[i] = q;
-            }
-            if (kx != 0) {
-                const int k0 = 32 * f + 16 * hh;   // this thread's first k_y
+            for (int h = 0; h < 2; ++h) {
+                float q[32];
+                if (h == 0) tcx::tmem_ld16x2_8x4<0, 32, 64, 96>(tlane, q);
+                else tcx::tmem_ld16x2_8x4<8, 40, 72, 104>(tlane, q);
+                if (kx == 0) {   // the k_x slot-0 rows for the packed bins
+                    const int b = f * 128 + 16 * hh + 8 * h;
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int kr = k0 + 8 * h, ki = 64 + k0 + 8 * h;
-                    put8<SPLIT>(dat, ((kx >> 3) * 16 + (kr >> 3)) * 128 + (kx & 7) * 16, pr + 8 * h);
-                    put8<SPLIT>(dat, ((kx >> 3) * 16 + (ki >> 3)) * 128 + (kx & 7) * 16, pi + 8 * h);
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int v4 = 0; v4 < 2; ++v4)
+                            *reinterpret_cast<float4*>(pk + b + 32 * u + 4 * v4) =
+                                make_float4(q[8 * u + 4 * v4], q[8 * u + 4 * v4 + 1], q[8 * u + 4 * v4 + 2],
+                                            q[8 * u + 4 * v4 + 3]);
+                }
+                float pr[8], pi[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const float mr = q[i], mn = q[16 + i];
+                    const float orr = __shfl_xor_sync(0xffffffffu, q[8 + i], 8);
+                    const float onn = __shfl_xor_sync(0xffffffffu, q[24 + i], 8);
+                    float r = fmaf(mr, orr, mn * onn);
+                    float qq = sq * fmaf(orr, mn, -(onn * mr));
+                    if (i & 1) { r = -r; qq = -qq; }   // quadrant sign (-1)^k_y
+                    if (MODE == kModeReal && i == 0 && hh == 0 && h == 0) { r = 0.f; qq = 0.f; }   // k_y = 0 or 32
+                    pr[i] = r;
+                    pi[i] = qq;
+                }
+                if (kx != 0) {
+                    const int kr = 32 * f + 16 * hh + 8 * h, ki = 64 + kr;
+                    put8<SPLIT>(dat, ((kx >> 3) * 16 + (kr >> 3)) * 128 + (kx & 7) * 16, pr);
+                    put8<SPLIT>(dat, ((kx >> 3) * 16 + (ki >> 3)) * 128 + (kx & 7) * 16, pi);
                 }
             }
             if (warp == 0) {   // the packed row k_x = 0 | 32, two k_y per lane
@@ -452,31 +448,30 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_before();
         gsync();
 
-        // ---- find_peaks: thread = (column x, 32-row block); rows roll
-        // through registers, neighbouring columns from the neighbouring lanes
-        // (the two edge lanes of a warp read theirs)
+        // ---- find_peaks: thread = (column x, 32-row block); the block's
+        // candidate rows roll through registers, neighbouring columns come
+        // from the neighbouring lanes (the two edge lanes of a warp read
+        // theirs); branch-free top two
         {
             const int xs = tid & 63, yb = (tid >> 6) * 32;
             const bool col_ok = xs >= SX0 && xs < SX1;
+            const int y0 = yb > SY0 ? yb : SY0, y1 = yb + 32 < SY1 ? yb + 32 : SY1;   // uniform over the warp
+            const int xl = (xs + W - 1) & (W - 1), xr = (xs + 1) & (W - 1);
             Top2 s{ TC_NEG_INF, TC_NEG_INF, 0x7fffffff };
-            float up = P[((yb + W - 1) & (W - 1)) * kPS + xs], cc = P[yb * kPS + xs];
+            float up = P[(y0 - 1) * kPS + xs], cc = P[y0 * kPS + xs];
 #pragma unroll 4
-            for (int ys = yb; ys < yb + 32; ++ys) {
-                const float dn = P[((ys + 1) & (W - 1)) * kPS + xs];
-                float lf = __shfl_up_sync(0xffffffffu, cc, 1);
-                float rt = __shfl_down_sync(0xffffffffu, cc, 1);
-                if (lane == 0) lf = P[ys * kPS + ((xs + W - 1) & (W - 1))];
-                if (lane == 31) rt = P[ys * kPS + ((xs + 1) & (W - 1))];
+            for (int ys = y0; ys < y1; ++ys) {
+                const float dn = P[(ys + 1) * kPS + xs];
+                const float sl = __shfl_up_sync(0xffffffffu, cc, 1);
+                const float sr = __shfl_down_sync(0xffffffffu, cc, 1);
+                const float lf = lane == 0 ? P[ys * kPS + xl] : sl;
+                const float rt = lane == 31 ? P[ys * kPS + xr] : sr;
                 const float m = tcx::fmax3(up, dn, fmaxf(lf, rt));
-                if (col_ok && ys >= SY0 && ys < SY1 && m < cc) {
-                    if (cc > s.t0) {
-                        s.t1 = s.t0;
-                        s.t0 = cc;
-                        s.key = ys * W + xs;
-                    } else {
-                        s.t1 = fmaxf(s.t1, cc);
-                    }
-                }
+                const float sv = (col_ok && m < cc) ? cc : TC_NEG_INF;
+                const bool gt = sv > s.t0;
+                s.t1 = gt ? s.t0 : fmaxf(s.t1, sv);
+                s.key = gt ? ys * W + xs : s.key;
+                s.t0 = gt ? sv : s.t0;
                 up = cc;
                 cc = dn;
             }
@@ -495,46 +490,60 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         }
         gsync();
 
-        // ---- fit_simple_gaussian and the vector (one thread)
-        if (tid == 0) {
+        // ---- fit_simple_gaussian and the vector: warp 0, the six
+        // logarithms on six lanes, relative to the pedestal
+        if (warp == 0) {
             Top2 s{ wt0[0], wt1[0], wkey[0] };
 #pragma unroll
             for (int i = 1; i < 4; ++i) top2_merge(s, wt0[i], wt1[i], wkey[i]);
             const int sum_a = wsum[0] + wsum[1], sum_b = wsum[2] + wsum[3];
-            const int gw = grow * p.gnx + gcol;
             // the pedestal for the fit in FP32 (the exact integer sums rounded
             // to float); REAL mode's plane has none
             const float ped = MODE == kModeReal ? 0.f : (float)sum_a * (float)sum_b;
-            opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
-            int32_t code = -1;
             const bool has2 = s.t1 > TC_NEG_INF;
-            int px = 0, py = 0;
-            if (has2) {
-                px = s.key & (W - 1);
-                py = s.key >> 6;
-                const float vc = P[py * kPS + px], vl = P[py * kPS + px - 1], vr = P[py * kPS + px + 1];
-                const float vu = P[(py - 1) * kPS + px], vd = P[(py + 1) * kPS + px];
-                const float C = vc + ped, Lv = vl + ped, R = vr + ped, U = vu + ped, D = vd + ped;
-                const float nan = __int_as_float(0x7fffffff);
-                const bool okx = Lv > 0.f && C > 0.f && R > 0.f;
-                const bool oky = U > 0.f && C > 0.f && D > 0.f;
-                // (ln L - ln R) / (2 (ln L + ln R - 2 ln C)) relative to C
-                const float fx = okx ? log1pf((vl - vr) / R) / (2.f * (log1pf((vl - vc) / C) + log1pf((vr - vc) / C)))
-                                     : nan;
-                const float fy = oky ? log1pf((vu - vd) / D) / (2.f * (log1pf((vu - vc) / C) + log1pf((vd - vc) / C)))
-                                     : nan;
-                const float p0 = s.t0 + ped, p1 = s.t1 + ped;
-                out.x = (float)(ox + W / 2);
-                out.y = (float)(p.img_h - (oy + W / 2));
-                out.u = (float)(W / 2 - px) - fx;
-                out.v = (float)(W / 2 - py) - fy;
-                out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
-                code = s.key;
+            const int px = s.key & (W - 1), py = (s.key >> 6) & (W - 1);
+            // lane j's logarithm: ln(L/R), ln(L/C), ln(R/C), ln(U/D), ln(U/C), ln(D/C)
+            const int j = lane < 6 ? lane : 0;
+            const int nx = (j == 2) ? px + 1 : (j < 2 ? px - 1 : px);
+            const int ny = (j == 3 || j == 4) ? py - 1 : (j == 5 ? py + 1 : py);
+            const int qx = (j == 0) ? px + 1 : px;
+            const int qy = (j == 3) ? py + 1 : py;
+            const float an = P[(ny & (W - 1)) * kPS + (nx & (W - 1))];
+            const float ad = P[(qy & (W - 1)) * kPS + (qx & (W - 1))];
+            const float lg = log1pf((an - ad) / (ad + ped));
+            const float lxr = __shfl_sync(0xffffffffu, lg, 0);
+            const float lxl = __shfl_sync(0xffffffffu, lg, 1);
+            const float lxrr = __shfl_sync(0xffffffffu, lg, 2);
+            const float lyd = __shfl_sync(0xffffffffu, lg, 3);
+            const float lyu = __shfl_sync(0xffffffffu, lg, 4);
+            const float lydd = __shfl_sync(0xffffffffu, lg, 5);
+            if (lane == 0) {
+                const int gw = grow * p.gnx + gcol;
+                opiv_vector out{ 0.f, 0.f, 0.f, 0.f, 0.f };
+                int32_t code = -1;
+                if (has2) {
+                    const float vc = P[py * kPS + px];
+                    const float C = vc + ped;
+                    const float Lv = P[py * kPS + px - 1] + ped, R = P[py * kPS + px + 1] + ped;
+                    const float U = P[(py - 1) * kPS + px] + ped, D = P[(py + 1) * kPS + px] + ped;
+                    const float nan = __int_as_float(0x7fffffff);
+                    const bool okx = Lv > 0.f && C > 0.f && R > 0.f;
+                    const bool oky = U > 0.f && C > 0.f && D > 0.f;
+                    const float fx = okx ? lxr / (2.f * (lxl + lxrr)) : nan;
+                    const float fy = oky ? lyd / (2.f * (lyu + lydd)) : nan;
+                    const float p0 = s.t0 + ped, p1 = s.t1 + ped;
+                    out.x = (float)(ox + W / 2);
+                    out.y = (float)(p.img_h - (oy + W / 2));
+                    out.u = (float)(W / 2 - px) - fx;
+                    out.v = (float)(W / 2 - py) - fy;
+                    out.sn = (p1 > 0.f) ? p0 / p1 : 0.f;
+                    code = s.key;
+                }
+                p.out_vec[gw] = out;
+                if (p.out_peak) p.out_peak[gw] = code;
+                if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
+                if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sum_a * (double)sum_b;
             }
-            p.out_vec[gw] = out;
-            if (p.out_peak) p.out_peak[gw] = code;
-            if (p.out_disp) p.out_disp[gw] = has2 ? pack_disp(px - W / 2, py - W / 2) : 0;
-            if (p.peds) p.peds[gw] = MODE == kModeReal ? 0.0 : (double)sum_a * (double)sum_b;
         }
         // the next window: the barrier after its pixel stage orders this
         // window's plane and tensor-memory reads before anything overwrites them

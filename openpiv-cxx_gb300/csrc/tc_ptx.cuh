@@ -197,6 +197,29 @@ __device__ __forceinline__ void tmem_ld16x2_16(uint32_t taddr, float* v)
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Four 8-column loads of the 16x32bx2 shape (half-split offset 16) under one
+// wait: threads 0-15 get columns c_i .. c_i + 7 of lanes taddr.lane + t,
+// threads 16-31 columns c_i + 16 .. c_i + 23, for c_i = taddr.col + o_i;
+// v[8 i + j] holds column j of load i.
+template <int O0, int O1, int O2, int O3>
+__device__ __forceinline__ void tmem_ld16x2_8x4(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.16x32bx2.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%32], 16;\n"
+                 "tcgen05.ld.sync.aligned.16x32bx2.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%33], 16;\n"
+                 "tcgen05.ld.sync.aligned.16x32bx2.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%34], 16;\n"
+                 "tcgen05.ld.sync.aligned.16x32bx2.x8.b32 {%24,%25,%26,%27,%28,%29,%30,%31}, [%35], 16;\n"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+                   "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+                   "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr + O0), "r"(taddr + O1), "r"(taddr + O2), "r"(taddr + O3) : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // max of three floats in one instruction (max.f32 with three sources)
 __device__ __forceinline__ float fmax3(float a, float b, float c)
 {
