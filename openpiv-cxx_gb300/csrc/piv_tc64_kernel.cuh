@@ -146,8 +146,8 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
     constexpr uint32_t kId1 = tcx::idesc_f16kind(128, 64, false, false);
     constexpr uint32_t kId2 = tcx::idesc_f16kind(64, 128, true, false);
-    constexpr uint32_t kId3 = tcx::idesc_f16kind(64, 128, false, false);
-    constexpr uint32_t kId4 = tcx::idesc_f16kind(64, 64, true, false);
+    constexpr uint32_t kId3 = tcx::idesc_f16kind(128, 32, false, false);
+    constexpr uint32_t kId4 = tcx::idesc_f16kind(64, 64, false, false);
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* cst = smem;
@@ -177,6 +177,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
     auto mat = [&](int m, int ks) { return dB + (uint64_t)((m * kMat + ks * 256) >> 4); };
     const uint64_t dMN = tcx::sdesc(dat_a, 1024, 128);
     const uint64_t dK3 = tcx::sdesc(dat_a, 128, 2048);
+    const uint64_t dK4 = tcx::sdesc(dat_a, 128, 1024);   // K-major, K = 64: 8 K groups per row group
     auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
 
     for (int i = threadIdx.x; i < (SPLIT ? 2 : 1) * kSet / 16; i += kThreads * kGroups)
@@ -380,44 +381,48 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         tcx::fence_before();
         gsync();
 
-        // ---- stage 3: inverse column DFT: the Re part against [C; S], the
-        // Im part against [-S; C] (M = 64, rows 32..63 unused, N = 128)
+        // ---- stage 3: inverse column DFT, transposed: T^T = [C; S] x Pr^T +
+        // [-S; C] x Pi^T with the constants as the A operand (M = 128 rows:
+        // Re T(y) then Im T(y)) and the products as the B operand (N = 32
+        // rows k_x, K-major as E2 wrote them, K = (Re | Im) x k_y = 128)
         if (tid == 0 && !p.mma_skip) {
             tcx::fence_after();
 #pragma unroll
-            for (int ks = 0; ks < 8; ++ks)
-                mma3<SPLIT>(tbase, dK3 + off(ks * 256), ks < 4 ? mat(kTcC, ks) : mat(kTcNS, ks - 4), kId3, ks > 0);
+            for (int ks = 0; ks < 8; ++ks) {
+                const uint64_t a = ks < 4 ? mat(kTcC, ks) : mat(kTcNS, ks - 4), b = dK3 + off(ks * 256);
+                tcx::mma_bf16(tbase, a, b, kId3, ks > 0);
+                if (SPLIT) {
+                    tcx::mma_bf16(tbase, a + (uint64_t)(kSet >> 4), b, kId3, true);
+                    tcx::mma_bf16(tbase, a, b + (uint64_t)(kLo >> 4), kId3, true);
+                }
+            }
             tcx::commit(mbar);
         }
         wait_mma();
 
-        // ---- E3: T into the stage-4 operand (MN-major, M = y', K = (Re |
-        // Im) x k_x = 64).  Warps 0 and 1 hold rows k_x = 16 warp + lane % 16;
-        // lane / 16 takes the columns y in [16 hh, +16) and [32 + 16 hh, +16).
-        if (warp < 2) {
-            const int L = lane & 15, hh = lane >> 4;
-            const int kx = 16 * warp + L;
-            float t[16];
+        // ---- E3: T into the stage-4 operand (K-major, M = y', K = (Re | Im)
+        // x k_x = 64, core matrix (row group, K group) at (y' / 8) * 1024 +
+        // (K / 8) * 128).  Thread tid holds accumulator row tid = part * 64 +
+        // y: the 32 values T_part(y, k_x).
+        {
+            const int part = tid >> 6, y = tid & 63;
+            float t[32];
+            tcx::tmem_ld32(tlane, t);
 #pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {   // Re y-lo, Re y-hi, Im y-lo, Im y-hi
-                tcx::tmem_ld16x2_16(tlane + 32 * c4, t);
-                const int part = c4 >> 1, y0 = 32 * (c4 & 1) + 16 * hh;
-                const int k = part * 32 + kx;
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    put8<SPLIT>(dat, (k >> 3) * 1024 + ((y0 >> 3) + h) * 128 + (k & 7) * 16, t + 8 * h);
-            }
+            for (int c = 0; c < 4; ++c)
+                put8<SPLIT>(dat, ((y >> 3) * 8 + part * 4 + c) * 128 + (y & 7) * 16, t + 8 * c);
         }
         tcx::fence_proxy();
         tcx::fence_before();
         gsync();
 
-        // ---- stage 4: real inverse row DFT, D = T * C4 (M = 64, N = 64, K = 64)
+        // ---- stage 4: real inverse row DFT, D = T * C4 (M = 64, N = 64,
+        // K = 64, the operand K-major)
         if (tid == 0 && !p.mma_skip) {
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dMN + off(ks * 2048), mat(kTcC4, ks), kId4, ks > 0);
+                mma3<SPLIT>(tbase, dK4 + off(ks * 256), mat(kTcC4, ks), kId4, ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
