@@ -19,8 +19,10 @@ cudaError_t launch_piv_tc_fp16x2(const PivParams& p, int dtype, int mode, int li
                                  cudaStream_t s);
 bool tc16_takes(const PivParams& p);
 bool tc64_takes(const PivParams& p);
-cudaError_t launch_piv_tc64(const PivParams& p, int dtype, int mode, int limit, bool split, const void* consts,
-                            cudaStream_t s);
+cudaError_t launch_piv_tc64_bf16(const PivParams& p, int dtype, int mode, int limit, bool split,
+                                 const void* consts, cudaStream_t s);
+cudaError_t launch_piv_tc64_fp16(const PivParams& p, int dtype, int mode, int limit, int passes,
+                                 const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tc16_bf16(const PivParams& p, int dtype, int mode, int limit, bool split,
                                  const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tc16_fp16(const PivParams& p, int dtype, int mode, int limit, int passes,
@@ -168,8 +170,10 @@ cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int li
     case 32: return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, set, s)
                          : launch_piv_tc_bf16(p, dtype, mode, limit, split, set, s);
     case 48: return launch_piv_tcg_w48(p, dtype, mode, limit, passes, fp16, set, s);
-    case 64:   // BF16 operands on grids at x multiples of 8: one window per tile
-        if (!fp16 && tc64_takes(p)) return launch_piv_tc64(p, dtype, mode, limit, split, set, s);
+    case 64:   // grids at x multiples of 8: one window per tile
+        if (tc64_takes(p))
+            return fp16 ? launch_piv_tc64_fp16(p, dtype, mode, limit, passes, set, s)
+                        : launch_piv_tc64_bf16(p, dtype, mode, limit, split, set, s);
         return launch_piv_tcg_w64(p, dtype, mode, limit, passes, fp16, set, s);
     default: return cudaErrorInvalidValue;
     }

@@ -1,16 +1,17 @@
-// Instantiations of the 64 px one-window-per-tile tensor-core kernel (BF16
-// operands, split or plain), and the test of its applicability.
+// Instantiations of the 64 px one-window-per-tile tensor-core kernel with
+// BF16 operands (split or plain), and the test of its applicability; the
+// FP16 instantiations are in piv_tc64_fp16.cu.
 #include "piv_tc64_kernel.cuh"
 
 namespace opiv {
 
 bool tc64_takes(const PivParams& p) { return tc64::applicable(p); }
 
-cudaError_t launch_piv_tc64(const PivParams& p, int dtype, int mode, int limit, bool split, const void* consts,
-                            cudaStream_t s)
+cudaError_t launch_piv_tc64_bf16(const PivParams& p, int dtype, int mode, int limit, bool split,
+                                 const void* consts, cudaStream_t s)
 {
-    return split ? tc64::by_mode<true>(p, dtype, mode, limit, consts, s)
-                 : tc64::by_mode<false>(p, dtype, mode, limit, consts, s);
+    return split ? tc64::by_mode<false, true, true>(p, dtype, mode, limit, consts, s)
+                 : tc64::by_mode<false, false, false>(p, dtype, mode, limit, consts, s);
 }
 
 }  // namespace opiv

@@ -71,49 +71,50 @@ static_assert(kGroups * kGroupCols <= 512, "tensor memory");
 static_assert(W * kPS * 4 <= kDataBytes, "plane in the data buffer");
 
 // 8 values into one 16-byte core-matrix row (hi, and lo kLo further)
-template <bool SPLIT>
+template <bool F16, bool SPLIT>
 __device__ __forceinline__ void put8(unsigned char* base, int off, const float* v)
 {
     if (SPLIT) {
         uint4 hi, lo;
-        split8<false>(v, hi, lo);
+        split8<F16>(v, hi, lo);
         *reinterpret_cast<uint4*>(base + off) = hi;
         *reinterpret_cast<uint4*>(base + kLo + off) = lo;
     } else {
-        *reinterpret_cast<uint4*>(base + off) = round8<false>(v);
+        *reinterpret_cast<uint4*>(base + off) = round8<F16>(v);
     }
 }
 
-template <bool SPLIT>
+template <bool F16, bool SPLIT>
 __device__ __forceinline__ void put1(unsigned char* base, int off, float v)
 {
-    const uint32_t h = pack2<false>(v, 0.f);
+    const uint32_t h = pack2<F16>(v, 0.f);
     *reinterpret_cast<uint16_t*>(base + off) = (uint16_t)(h & 0xffffu);
     if (SPLIT) {
-        const float hv = unpack2<false>(h).x;
-        *reinterpret_cast<uint16_t*>(base + kLo + off) = (uint16_t)(pack2<false>(v - hv, 0.f) & 0xffffu);
+        const float hv = unpack2<F16>(h).x;
+        *reinterpret_cast<uint16_t*>(base + kLo + off) = (uint16_t)(pack2<F16>(v - hv, 0.f) & 0xffffu);
     }
 }
 
-// D (+)= A * B split into hi*hi, hi*lo, lo*hi (a, b: descriptors of the hi
-// parts; the data's lo part kLo further, the constants' one set further)
-template <bool SPLIT>
+// D (+)= A * B split into hi*hi, hi*lo (CSPLIT: the constant's lo part),
+// lo*hi (a, b: descriptors of the hi parts; the data's lo part kLo further,
+// the constants' one set further)
+template <bool SPLIT, bool CSPLIT>
 __device__ __forceinline__ void mma3(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, bool acc)
 {
     tcx::mma_bf16(d, a, b, idesc, acc);
     if (SPLIT) {
-        tcx::mma_bf16(d, a, b + (uint64_t)(kSet >> 4), idesc, true);
+        if (CSPLIT) tcx::mma_bf16(d, a, b + (uint64_t)(kSet >> 4), idesc, true);
         tcx::mma_bf16(d, a + (uint64_t)(kLo >> 4), b, idesc, true);
     }
 }
 
-template <bool SPLIT>
+template <bool SPLIT, bool CSPLIT>
 __device__ __forceinline__ void mma3_ta(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint64_t b, uint32_t idesc,
                                         bool acc)
 {
     tcx::mma_bf16_ta(d, a_hi, b, idesc, acc);
     if (SPLIT) {
-        tcx::mma_bf16_ta(d, a_hi, b + (uint64_t)(kSet >> 4), idesc, true);
+        if (CSPLIT) tcx::mma_bf16_ta(d, a_hi, b + (uint64_t)(kSet >> 4), idesc, true);
         tcx::mma_bf16_ta(d, a_lo, b, idesc, true);
     }
 }
@@ -134,20 +135,28 @@ __device__ __forceinline__ void top2_merge(Top2& s, float o0, float o1, int ok)
     s.t1 = n1;
 }
 
-template <bool SPLIT, int MODE, bool LIMIT, typename PixT>
+// F16: FP16 operands scaled by powers of two as in the other tensor-core
+// kernels (pixels x 2^-4, the stage-1 matrix x 2^-9 in the constants, the
+// products x 2^-e with e per window from its largest product, T x 2^-6),
+// undone exactly in the peak stage.  CSPLIT: the constants' lo parts enter
+// too (three MMAs per product); otherwise only the data is split (two).
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT>
 __global__ void __launch_bounds__(kThreads * kGroups, 1)
 piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
 {
+    constexpr float kPix = F16 ? 0.0625f : 1.f;
+    constexpr float kT = F16 ? 0.015625f : 1.f;
+    constexpr float kSumUnscale = F16 ? 8192.f : 1.f;
     // peak scan range in swapped-plane coordinates (image_utils.impl.h:48,
     // :54; limited search: rect::dilate(0.5), rect.cpp:109-126)
     constexpr int D0 = LIMIT ? W / 4 : 0;
     constexpr int VW = LIMIT ? W / 2 : W;
     constexpr int SY0 = D0 + 1, SY1 = D0 + VW - 2;
     constexpr int SX0 = D0 + 1, SX1 = D0 + VW - 1;
-    constexpr uint32_t kId1 = tcx::idesc_f16kind(128, 64, false, false);
-    constexpr uint32_t kId2 = tcx::idesc_f16kind(64, 128, true, false);
-    constexpr uint32_t kId3 = tcx::idesc_f16kind(128, 32, false, false);
-    constexpr uint32_t kId4 = tcx::idesc_f16kind(64, 64, false, false);
+    constexpr uint32_t kId1 = tcx::idesc_f16kind(128, 64, false, F16);
+    constexpr uint32_t kId2 = tcx::idesc_f16kind(64, 128, true, F16);
+    constexpr uint32_t kId3 = tcx::idesc_f16kind(128, 32, false, F16);
+    constexpr uint32_t kId4 = tcx::idesc_f16kind(64, 64, false, F16);
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* cst = smem;
@@ -160,7 +169,8 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
     float* wt1 = wt0 + 4;
     int* wkey = reinterpret_cast<int*>(wt1 + 4);
     int* wsum = wkey + 4;                                   // per-warp pixel sums
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(wsum + 4);
+    float* wmax = reinterpret_cast<float*>(wsum + 4);       // F16: per-warp largest product
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(wmax + 4);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
     int* abort_flag = reinterpret_cast<int*>(tslot + 1);
     // the CTA's tensor-memory address lives in group 0's tail
@@ -180,7 +190,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
     const uint64_t dK4 = tcx::sdesc(dat_a, 128, 1024);   // K-major, K = 64: 8 K groups per row group
     auto off = [](int bytes) { return (uint64_t)(bytes >> 4); };
 
-    for (int i = threadIdx.x; i < (SPLIT ? 2 : 1) * kSet / 16; i += kThreads * kGroups)
+    for (int i = threadIdx.x; i < (CSPLIT ? 2 : 1) * kSet / 16; i += kThreads * kGroups)
         reinterpret_cast<uint4*>(cst)[i] = consts[i];
     if (tid == 0) {
         tcx::mbar_init(mbar, 1);
@@ -224,7 +234,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         {
             const int f = tid >> 6, y = tid & 63;
             const PixT* row = (f ? fb : fa) + (size_t)(oy + y) * pitch + ox;
-            const float sg = (f && (y & 1)) ? -1.f : 1.f;
+            const float sg = ((f && (y & 1)) ? -1.f : 1.f) * kPix;
 #pragma unroll
             for (int hp = 0; hp < 2; ++hp) {   // pixels 32 hp .. 32 hp + 31: columns 16 hp .. + 15
                 uint32_t hw[16], lw[16];
@@ -234,10 +244,10 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
                     widen8<PixT>(tc::load_raw<PixT>(row + 32 * hp + 8 * g), px, sg);
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        hw[4 * g + j] = pack2<false>(px[2 * j], px[2 * j + 1]);
+                        hw[4 * g + j] = pack2<F16>(px[2 * j], px[2 * j + 1]);
                         if (SPLIT) {
-                            const float2 hf = unpack2<false>(hw[4 * g + j]);
-                            lw[4 * g + j] = pack2<false>(px[2 * j] - hf.x, px[2 * j + 1] - hf.y);
+                            const float2 hf = unpack2<F16>(hw[4 * g + j]);
+                            lw[4 * g + j] = pack2<F16>(px[2 * j] - hf.x, px[2 * j + 1] - hf.y);
                         }
                     }
                 }
@@ -254,7 +264,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
-                mma3_ta<SPLIT>(tbase, tbase + kA1 + 8 * ks, tbase + kA1 + 32 + 8 * ks, mat(kTcG1, ks), kId1,
+                mma3_ta<SPLIT, CSPLIT>(tbase, tbase + kA1 + 8 * ks, tbase + kA1 + 32 + 8 * ks, mat(kTcG1, ks), kId1,
                                ks > 0);
             tcx::commit(mbar);
         }
@@ -280,7 +290,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
                 if (part == 0) rs[f * 64 + y] = (f && (y & 1)) ? -c[0] : c[0];   // undo the frame-B row sign
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    put8<SPLIT>(dat, (part * 8 + (y >> 3)) * 1024 + (2 * j + f) * 128 + (y & 7) * 16, c + 8 * j);
+                    put8<F16, SPLIT>(dat, (part * 8 + (y >> 3)) * 1024 + (2 * j + f) * 128 + (y & 7) * 16, c + 8 * j);
             }
         }
         tcx::fence_proxy();
@@ -293,7 +303,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 8; ++ks)
-                mma3<SPLIT>(tbase, dMN + off(ks * 2048), ks < 4 ? mat(kTcC, ks) : mat(kTcNS, ks - 4), kId2, ks > 0);
+                mma3<SPLIT, CSPLIT>(tbase, dMN + off(ks * 2048), ks < 4 ? mat(kTcC, ks) : mat(kTcNS, ks - 4), kId2, ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -301,33 +311,37 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
         // ---- E2: products into the stage-3 operand (K-major, rows k_x,
         // K = (Re | Im) x k_y = 128).  Thread: row L = lane % 16 of warp j
         // (frame L / 8, k_x = 8 j + L % 8), column half hh = lane / 16.
+        int escale = 0;   // F16: the window's product exponent
         {
             const int L = lane & 15, hh = lane >> 4;
             const int f = L >> 3, kx = 8 * warp + (L & 7);
             float* pk = reinterpret_cast<float*>(dat + kPacked);   // [frame][Re 64 | -Im 64]
             const float sq = f ? -1.f : 1.f;
-            // frame a's thread computes k_y = 16 hh + 8 h + i, frame b's 32 more
-            // (h: the half, i < 8); frame b's columns are rotated by 32, so
-            // both find their own values in q[i], q[16 + i] (Re, -Im) and take
-            // their partner's (lane ^ 8) q[8 + i], q[24 + i].  With m = own,
-            // o = partner values and n = -Im: Re P = m_r o_r + m_n o_n,
-            // Im P = +-(o_r m_n - o_n m_r), + for frame a.
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float q[32];
+            // half h: columns 16 hh + 8 h + i of each quarter (i < 8): q[i] Re,
+            // q[8 + i] Re 32 further, q[16 + i] -Im, q[24 + i] -Im 32 further
+            auto load_half = [&](int h, float* q) {
                 if (h == 0) tcx::tmem_ld16x2_8x4<0, 32, 64, 96>(tlane, q);
                 else tcx::tmem_ld16x2_8x4<8, 40, 72, 104>(tlane, q);
-                if (kx == 0) {   // the k_x slot-0 rows for the packed bins
-                    const int b = f * 128 + 16 * hh + 8 * h;
+            };
+            auto keep_slot0 = [&](int h, const float* q) {   // the k_x slot-0 rows for the packed bins
+                if (kx == 0) {
+                    const int b0 = f * 128 + 16 * hh + 8 * h;
 #pragma unroll
                     for (int u = 0; u < 4; ++u)
 #pragma unroll
                         for (int v4 = 0; v4 < 2; ++v4)
-                            *reinterpret_cast<float4*>(pk + b + 32 * u + 4 * v4) =
+                            *reinterpret_cast<float4*>(pk + b0 + 32 * u + 4 * v4) =
                                 make_float4(q[8 * u + 4 * v4], q[8 * u + 4 * v4 + 1], q[8 * u + 4 * v4 + 2],
                                             q[8 * u + 4 * v4 + 3]);
                 }
-                float pr[8], pi[8];
+            };
+            // frame a's thread computes k_y = 16 hh + 8 h + i, frame b's 32 more;
+            // frame b's columns are rotated by 32, so both find their own
+            // values in q[i], q[16 + i] and take their partner's (lane ^ 8)
+            // q[8 + i], q[24 + i].  With m = own, o = partner values and
+            // n = -Im: Re P = m_r o_r + m_n o_n, Im P = +-(o_r m_n - o_n m_r),
+            // + for frame a.
+            auto products = [&](int h, const float* q, float* pr, float* pi) {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const float mr = q[i], mn = q[16 + i];
@@ -340,40 +354,104 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
                     pr[i] = r;
                     pi[i] = qq;
                 }
+            };
+            auto store_half = [&](int h, const float* pr, const float* pi) {
                 if (kx != 0) {
                     const int kr = 32 * f + 16 * hh + 8 * h, ki = 64 + kr;
-                    put8<SPLIT>(dat, ((kx >> 3) * 16 + (kr >> 3)) * 128 + (kx & 7) * 16, pr);
-                    put8<SPLIT>(dat, ((kx >> 3) * 16 + (ki >> 3)) * 128 + (kx & 7) * 16, pi);
+                    put8<F16, SPLIT>(dat, ((kx >> 3) * 16 + (kr >> 3)) * 128 + (kx & 7) * 16, pr);
+                    put8<F16, SPLIT>(dat, ((kx >> 3) * 16 + (ki >> 3)) * 128 + (kx & 7) * 16, pi);
                 }
-            }
-            if (warp == 0) {   // the packed row k_x = 0 | 32, two k_y per lane
-                __syncwarp();
+            };
+            // the packed row k_x = 0 | 32 (warp 0, k_y = lane + 32 h2)
+            auto packed = [&](int h2, float& pkr, float& pkq) {
                 const float* sa = pk;          // frame a, k_x slot 0
                 const float* sb = pk + 128;    // frame b, columns rotated by 32
+                const int ky = lane + 32 * h2, kn = (64 - ky) & 63;
+                const int kb = (ky + 32) & 63, kbn = (kn + 32) & 63;
+                // Z[k] = Re + i Im with Im = -stored
+                const float zar = sa[ky], zai = -sa[64 + ky], zanr = sa[kn], zani = -sa[64 + kn];
+                const float zbr = sb[kb], zbi = -sb[64 + kb], zbnr = sb[kbn], zbni = -sb[64 + kbn];
+                // X0 = (Z[k] + conj Z[-k]) / 2, X32 = i (Z[k] - conj Z[-k]) / 2
+                const float a0r = 0.5f * (zar + zanr), a0i = 0.5f * (zai - zani);
+                const float a6r = -0.5f * (zai + zani), a6i = 0.5f * (zar - zanr);
+                const float b0r = 0.5f * (zbr + zbnr), b0i = 0.5f * (zbi - zbni);
+                const float b6r = -0.5f * (zbi + zbni), b6i = 0.5f * (zbr - zbnr);
+                float p0r = b0r * a0r + b0i * a0i, p0i = b0i * a0r - b0r * a0i;
+                float p6r = b6r * a6r + b6i * a6i, p6i = b6i * a6r - b6r * a6i;
+                if (MODE == kModeReal) {
+                    p0r = 0.f; p0i = 0.f;
+                    if (ky == 0 || ky == H) { p6r = 0.f; p6i = 0.f; }
+                } else if (ky == 0) {
+                    p0r = 0.f; p0i = 0.f;         // pedestal removed
+                }
+                pkr = p0r - p6i;
+                pkq = p0i + p6r;
+                if (ky & 1) { pkr = -pkr; pkq = -pkq; }
+            };
+            auto store_packed = [&](int h2, float pkr, float pkq) {
+                const int ky = lane + 32 * h2;
+                put1<F16, SPLIT>(dat, (ky >> 3) * 128 + (ky & 7) * 2, pkr);
+                put1<F16, SPLIT>(dat, ((64 + ky) >> 3) * 128 + (ky & 7) * 2, pkq);
+            };
+            float sc = 1.f;
+            if constexpr (F16) {
+                // first the window's largest product over all four warps, so
+                // that the products scaled by 2^-e lie below 2^9 (stage 3 sums
+                // 128 of them into FP32; T x 2^-6 then fits FP16)
+                float m = 0.f;
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int ky = lane + 32 * h, kn = (64 - ky) & 63;
-                    const int kb = (ky + 32) & 63, kbn = (kn + 32) & 63;
-                    // Z[k] = Re + i Im with Im = -stored
-                    const float zar = sa[ky], zai = -sa[64 + ky], zanr = sa[kn], zani = -sa[64 + kn];
-                    const float zbr = sb[kb], zbi = -sb[64 + kb], zbnr = sb[kbn], zbni = -sb[64 + kbn];
-                    // X0 = (Z[k] + conj Z[-k]) / 2, X32 = i (Z[k] - conj Z[-k]) / 2
-                    const float a0r = 0.5f * (zar + zanr), a0i = 0.5f * (zai - zani);
-                    const float a6r = -0.5f * (zai + zani), a6i = 0.5f * (zar - zanr);
-                    const float b0r = 0.5f * (zbr + zbnr), b0i = 0.5f * (zbi - zbni);
-                    const float b6r = -0.5f * (zbi + zbni), b6i = 0.5f * (zbr - zbnr);
-                    float p0r = b0r * a0r + b0i * a0i, p0i = b0i * a0r - b0r * a0i;
-                    float p6r = b6r * a6r + b6i * a6i, p6i = b6i * a6r - b6r * a6i;
-                    if (MODE == kModeReal) {
-                        p0r = 0.f; p0i = 0.f;
-                        if (ky == 0 || ky == H) { p6r = 0.f; p6i = 0.f; }
-                    } else if (ky == 0) {
-                        p0r = 0.f; p0i = 0.f;         // pedestal removed
+                    float q[32], pr[8], pi[8];
+                    load_half(h, q);
+                    keep_slot0(h, q);
+                    products(h, q, pr, pi);
+                    if (kx != 0) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) m = fmaxf(m, fmaxf(fabsf(pr[i]), fabsf(pi[i])));
                     }
-                    float pkr = p0r - p6i, pkq = p0i + p6r;
-                    if (ky & 1) { pkr = -pkr; pkq = -pkq; }
-                    put1<SPLIT>(dat, (ky >> 3) * 128 + (ky & 7) * 2, pkr);
-                    put1<SPLIT>(dat, ((64 + ky) >> 3) * 128 + (ky & 7) * 2, pkq);
+                }
+                if (warp == 0) {
+                    __syncwarp();
+#pragma unroll
+                    for (int h2 = 0; h2 < 2; ++h2) {
+                        float a2, b2;
+                        packed(h2, a2, b2);
+                        m = fmaxf(m, fmaxf(fabsf(a2), fabsf(b2)));
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+                if (lane == 0) wmax[warp] = m;
+                gsync();
+                const float mm = fmaxf(fmaxf(wmax[0], wmax[1]), fmaxf(wmax[2], wmax[3]));
+                const int eb = (int)((__float_as_uint(mm) >> 23) & 0xffu);
+                int e = eb == 0 ? 0 : eb - 127 - 8;
+                e = e < -90 ? -90 : (e > 80 ? 80 : e);
+                escale = e;
+                sc = __uint_as_float((uint32_t)(127 - e) << 23);
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float q[32], pr[8], pi[8];
+                load_half(h, q);
+                if (!F16) keep_slot0(h, q);
+                products(h, q, pr, pi);
+                if (F16) {
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        pr[i] *= sc;
+                        pi[i] *= sc;
+                    }
+                }
+                store_half(h, pr, pi);
+            }
+            if (warp == 0) {
+                __syncwarp();
+#pragma unroll
+                for (int h2 = 0; h2 < 2; ++h2) {
+                    float a2, b2;
+                    packed(h2, a2, b2);
+                    store_packed(h2, a2 * sc, b2 * sc);
                 }
             }
         }
@@ -392,7 +470,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
                 const uint64_t a = ks < 4 ? mat(kTcC, ks) : mat(kTcNS, ks - 4), b = dK3 + off(ks * 256);
                 tcx::mma_bf16(tbase, a, b, kId3, ks > 0);
                 if (SPLIT) {
-                    tcx::mma_bf16(tbase, a + (uint64_t)(kSet >> 4), b, kId3, true);
+                    if (CSPLIT) tcx::mma_bf16(tbase, a + (uint64_t)(kSet >> 4), b, kId3, true);
                     tcx::mma_bf16(tbase, a, b + (uint64_t)(kLo >> 4), kId3, true);
                 }
             }
@@ -408,9 +486,13 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
             const int part = tid >> 6, y = tid & 63;
             float t[32];
             tcx::tmem_ld32(tlane, t);
+            if (F16) {
+#pragma unroll
+                for (int i = 0; i < 32; ++i) t[i] *= kT;
+            }
 #pragma unroll
             for (int c = 0; c < 4; ++c)
-                put8<SPLIT>(dat, ((y >> 3) * 8 + part * 4 + c) * 128 + (y & 7) * 16, t + 8 * c);
+                put8<F16, SPLIT>(dat, ((y >> 3) * 8 + part * 4 + c) * 128 + (y & 7) * 16, t + 8 * c);
         }
         tcx::fence_proxy();
         tcx::fence_before();
@@ -422,7 +504,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
             tcx::fence_after();
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks)
-                mma3<SPLIT>(tbase, dK4 + off(ks * 256), mat(kTcC4, ks), kId4, ks > 0);
+                mma3<SPLIT, CSPLIT>(tbase, dK4 + off(ks * 256), mat(kTcC4, ks), kId4, ks > 0);
             tcx::commit(mbar);
         }
         wait_mma();
@@ -435,6 +517,11 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
             const int y = 16 * warp + L;
             float v[32];
             tcx::tmem_ld16x2_32(tlane, v);
+            if (F16) {   // undo 2^-26 (pixels, stage-1 matrix, twice), 2^-e (products), 2^-6 (T)
+                const float us = __uint_as_float((uint32_t)(127 + 32 + escale) << 23);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] *= us;
+            }
 #pragma unroll
             for (int i = 0; i < 32; ++i) P[y * kPS + 32 * hh + i] = v[i];
             if (p.planes) {
@@ -445,7 +532,7 @@ piv_tc64_kernel(const PivParams p, const uint4* __restrict__ consts)
                         make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
             }
             // pixel sums: warps 0, 1 frame a, warps 2, 3 frame b (row 64 f + y)
-            int s = __float2int_rn(rs[tid]);
+            int s = __float2int_rn(rs[tid] * kSumUnscale);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) wsum[warp] = s;
@@ -571,10 +658,10 @@ inline bool applicable(const PivParams& p)
            p.prev_disp == nullptr;
 }
 
-template <bool SPLIT, int MODE, bool LIMIT, typename PixT>
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT>
 cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
 {
-    auto kern = piv_tc64_kernel<SPLIT, MODE, LIMIT, PixT>;
+    auto kern = piv_tc64_kernel<F16, SPLIT, CSPLIT, MODE, LIMIT, PixT>;
     static std::atomic<uint64_t> attr_done{ 0 };   // one bit per device
     static std::atomic<int> sm_count[64];
     int dev = 0;
@@ -597,21 +684,21 @@ cudaError_t launch_t(const PivParams& p, const void* consts, cudaStream_t s)
     return cudaGetLastError();
 }
 
-template <bool SPLIT, int MODE, bool LIMIT>
+template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT>
 cudaError_t by_dtype(const PivParams& p, int dtype, const void* consts, cudaStream_t s)
 {
-    return dtype == kU8 ? launch_t<SPLIT, MODE, LIMIT, uint8_t>(p, consts, s)
-                        : launch_t<SPLIT, MODE, LIMIT, uint16_t>(p, consts, s);
+    return dtype == kU8 ? launch_t<F16, SPLIT, CSPLIT, MODE, LIMIT, uint8_t>(p, consts, s)
+                        : launch_t<F16, SPLIT, CSPLIT, MODE, LIMIT, uint16_t>(p, consts, s);
 }
 
-template <bool SPLIT>
+template <bool F16, bool SPLIT, bool CSPLIT>
 cudaError_t by_mode(const PivParams& p, int dtype, int mode, int limit, const void* consts, cudaStream_t s)
 {
     if (mode == kModeReal)
-        return limit ? by_dtype<SPLIT, kModeReal, true>(p, dtype, consts, s)
-                     : by_dtype<SPLIT, kModeReal, false>(p, dtype, consts, s);
-    return limit ? by_dtype<SPLIT, kModeComplex, true>(p, dtype, consts, s)
-                 : by_dtype<SPLIT, kModeComplex, false>(p, dtype, consts, s);
+        return limit ? by_dtype<F16, SPLIT, CSPLIT, kModeReal, true>(p, dtype, consts, s)
+                     : by_dtype<F16, SPLIT, CSPLIT, kModeReal, false>(p, dtype, consts, s);
+    return limit ? by_dtype<F16, SPLIT, CSPLIT, kModeComplex, true>(p, dtype, consts, s)
+                 : by_dtype<F16, SPLIT, CSPLIT, kModeComplex, false>(p, dtype, consts, s);
 }
 
 }  // namespace tc64
