@@ -158,7 +158,9 @@ int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
  *   with row steps of 1..6 pixels and window x positions and x step on
  *   multiples of 4 pixels run a kernel that stacks eight windows of a grid
  *   column per tile (each image row transformed once); other 16 px grids a
- *   generic kernel (about half as fast).
+ *   generic kernel (about half as fast).  64 px grids with window x
+ *   positions and x step on multiples of 8 pixels run a kernel with one
+ *   window per tile (about three times the generic kernel's speed).
  * OPIV_PREC_TC_BF16: the same with plain BF16 operands (one MMA per product).
  * OPIV_PREC_TC_SPLIT_FP16 / OPIV_PREC_TC_FP16: the same with FP16 operands
  *   (11-bit significand), kept inside FP16's range by powers of two (a
