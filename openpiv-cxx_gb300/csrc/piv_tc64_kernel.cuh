@@ -1,6 +1,6 @@
-// Tensor-core (tcgen05) PIV window path for 64 x 64 windows, BF16 operands
-// (split hi/lo or plain), one window per tile (kernel templates;
-// instantiated in piv_tc64.cu): the 2-D cross-correlation of every window
+// Tensor-core (tcgen05) PIV window path for 64 x 64 windows, one window per
+// tile, BF16 or FP16 operands, split or plain (kernel templates; instantiated
+// in piv_tc64.cu and piv_tc64_fp16.cu): the 2-D cross-correlation of every window
 // pair as four chained DFT matrix products (FFT::cross_correlate,
 // fft.h:188-206, unnormalised), then find_peaks(plane, 2, 1), the 3-point
 // Gaussian fit and the vector (image_utils.impl.h:42-101, main.cpp:214-236).
@@ -15,7 +15,8 @@
 //            the slot k_x = 0, DC removed (the pedestal sum(a) sum(b) is
 //            added back in the fit), (-1)^k_y for the row quadrant swap,
 //            REAL mode's zeroed spectrum rows 0 and 32 and column 0.
-//   stage 3  inverse column DFT over k_y (rows k_x, N = (Re | Im) x y).
+//   stage 3  inverse column DFT over k_y, transposed: the constants as the
+//            A operand, the products (rows k_x) as the B operand.
 //   stage 4  real inverse row DFT over k_x, the weights and the column
 //            quadrant swap folded into the constant matrix C4.
 //
@@ -26,7 +27,7 @@
 // (M = 64 rows sit in lanes 32 (r / 16) + r % 16):
 //   stage 1  R = f * 64 + y (thread tid owns lane tid)
 //   stage 2  16 j + 8 f + (k_x & 7), j = k_x / 8: warp j, lanes 8 f + k_x % 8
-//   stage 3  k_x (0..31): warps 0 and 1, lanes 0..15; rows 32..63 unused
+//   stage 3  (Re | Im) x y (thread tid owns lane tid), N = 32 columns k_x
 //   stage 4  y' (0..63): warp y' / 16, lanes y' % 16
 // The plane goes to shared memory and is scanned by columns (rows rolling
 // through registers, neighbouring columns from the neighbouring lanes).
