@@ -326,19 +326,40 @@ def test_tc16_limited_search_u16(mode):
             assert rms <= rms_t and mx <= max_t and mm <= mm_t, (dx, dy, precision, rms, mx, mm)
 
 
+@pytest.mark.parametrize("ia,step", [(16, 4), (64, 16)])
 @pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
-def test_tc16_blank_frames(mode):
-    """Blank frames through the 16 px vertical-tile kernel: every plane is
-    zero, no strict maximum anywhere, so every vector is zero and every peak
-    code -1 (the reference's find_peaks returns fewer than two peaks)."""
+def test_blank_frames_16_64(ia, step, mode):
+    """Blank frames through the 16 px vertical-tile and the 64 px
+    one-window-per-tile kernels: every plane is zero, no strict maximum
+    anywhere, so every vector is zero and every peak code -1 (the
+    reference's find_peaks returns fewer than two peaks)."""
     a = np.zeros((256, 256), np.uint16)
     for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16, og.PREC_TC_BF16):
-        plan = og.Plan(256, 256, np.uint16, 16, 4, mode=mode)
+        plan = og.Plan(256, 256, np.uint16, ia, step, mode=mode)
         plan.set_precision(precision)
         vec, pk = plan.process(a, a)
         plan.status()
-        assert np.all(vec == 0) and np.all(pk == -1), precision
+        assert np.all(vec == 0) and np.all(pk == -1), (ia, precision)
         plan.close()
+
+
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_generic_kernel_64px_unaligned_grid(mode):
+    """64 px windows at an x step of 12 pixels (not a multiple of 8) run the
+    generic kernel: its planes against numpy's FP64 correlation and its
+    vectors against the FP64 pass, split BF16 and the FP16 data split."""
+    a, b = synth.config2(size=1024)
+    a, b = np.ascontiguousarray(a[:512, :512]), np.ascontiguousarray(b[:512, :512])
+    ref = run(a, b, 12, og.PREC_FP64, mode=mode, ia=64)
+    for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16):
+        got = run(a, b, 12, precision, mode=mode, planes=True, ia=64)
+        planes, ped = reference_planes(a, b, got["grid"], 64, mode)
+        assert np.array_equal(got["ped"], ped)
+        err = np.abs(got["planes"] - planes).max(axis=(1, 2)) / np.abs(planes).max(axis=(1, 2))
+        assert err.max() <= GENERIC_PLANE_RTOL[precision], (precision, err.max())
+        rms, mx, mm = displacement_error(got, ref)
+        rms_t, max_t, mm_t = BOUNDS[precision]
+        assert rms <= rms_t and mx <= max_t and mm <= mm_t, (precision, rms, mx, mm)
 
 
 def test_generic_limited_search_and_errors():
