@@ -72,24 +72,42 @@ def run(a, b, step, precision, mode=og.CORR_COMPLEX, limit=False, planes=False, 
     return out
 
 
-def fp64_reference(a, b, step, ia, mode, orc):
+def fp64_reference(a, b, step, ia, mode, orc, limit=False):
     """Vectors of the reference's chain on numpy FP64 planes (any window
-    size): find_peaks(plane, 2, 1), fit_simple_gaussian, main.cpp:220-236."""
+    size): find_peaks(plane, 2, 1), fit_simple_gaussian, main.cpp:220-236.
+    limit: the peak search on the central ia/2 x ia/2 view of the plane
+    (the search rectangle dilated by 0.5, rect.cpp:109-126), the fit on the
+    whole plane."""
     h, w = a.shape
     grid = orc.grid_offsets(w, h, ia, ia, step, step)
     planes, ped = reference_planes(a, b, grid, ia, mode)
     vec = np.zeros((len(grid), 5))
     peak = np.full(len(grid), -1, np.int64)
+    d0, vw = (ia // 4, ia // 2) if limit else (0, ia)
     for i, (x, y) in enumerate(grid):
         plane = planes[i] + ped[i]
-        xy, v = orc.find_peaks(plane, 2, 1)
+        xy, v = orc.find_peaks(np.ascontiguousarray(plane[d0:d0 + vw, d0:d0 + vw]), 2, 1)
         if len(v) < 2:
             continue
+        xy = xy + d0
         fx, fy = orc.fit_simple_gaussian(plane, int(xy[0, 0]), int(xy[0, 1]))
         mx, my = x + ia // 2, y + ia // 2
         vec[i] = (mx, h - my, mx - (x + fx), my - (y + fy), v[0] / v[1] if v[1] > 0 else 0.0)
         peak[i] = xy[0, 1] * ia + xy[0, 0]
     return {"vec": vec, "peak": peak, "grid": grid}
+
+
+def assert_near_ties(got, ref, planes, rtol, ctx):
+    """A peak that differs from the reference's is allowed only at a
+    near-tie that the operands' rounding can flip: the FP64 plane at the
+    kernel's peak within twice the plane tolerance rtol of the reference's
+    peak (a second peak of nearly the same height, or a neighbour of nearly
+    the same height when the displacement is close to half a pixel)."""
+    for i in np.flatnonzero(got["peak"] != ref["peak"]):
+        gp, rp = got["peak"][i], ref["peak"][i]
+        assert gp >= 0 and rp >= 0, (ctx, i, gp, rp)
+        drop = (planes[i].flat[rp] - planes[i].flat[gp]) / np.abs(planes[i]).max()
+        assert drop <= 2 * rtol, (ctx, i, gp, rp, drop)
 
 
 def displacement_error(got, ref):
@@ -248,7 +266,9 @@ def test_precision_sweep_variants(variant):
         assert rms <= rms_t and mx <= max_t and mm <= mm_t, (variant, precision, rms, mx, mm)
 
 
-# ---- 16, 48 and 64 px windows: the generic tensor-core kernel ---------------------
+# ---- 16, 48 and 64 px windows: the dedicated kernels where the grid allows them
+# (16 px: x on multiples of 4, row steps up to 6; 48 px: any regular grid;
+# 64 px: x on multiples of 8), else the generic tensor-core kernel ------------
 GENERIC = [(16, 8), (48, 24), (64, 32)]        # window, step on the 1024^2 u8 pair
 GENERIC_PLANE_RTOL = {og.PREC_TC_SPLIT_BF16: 5e-5, og.PREC_TC_BF16: 2e-2,
                       og.PREC_TC_SPLIT_FP16: 1e-4, og.PREC_TC_FP16: 5e-3,
@@ -326,21 +346,51 @@ def test_tc16_limited_search_u16(mode):
             assert rms <= rms_t and mx <= max_t and mm <= mm_t, (dx, dy, precision, rms, mx, mm)
 
 
-@pytest.mark.parametrize("ia,step", [(16, 4), (64, 16)])
+@pytest.mark.parametrize("ia,step", [(16, 4), (48, 12), (64, 16)])
 @pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
-def test_blank_frames_16_64(ia, step, mode):
-    """Blank frames through the 16 px vertical-tile and the 64 px
+def test_blank_frames_16_48_64(ia, step, mode):
+    """Blank frames through the 16 px vertical-tile and the 48 and 64 px
     one-window-per-tile kernels: every plane is zero, no strict maximum
     anywhere, so every vector is zero and every peak code -1 (the
     reference's find_peaks returns fewer than two peaks)."""
     a = np.zeros((256, 256), np.uint16)
     for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16, og.PREC_TC_BF16):
-        plan = og.Plan(256, 256, np.uint16, ia, step, mode=mode)
-        plan.set_precision(precision)
+        if ia == 48:
+            plan = og.Plan(256, 256, np.uint16, ia, step, mode=mode, tensor_core=precision)
+        else:
+            plan = og.Plan(256, 256, np.uint16, ia, step, mode=mode)
+            plan.set_precision(precision)
         vec, pk = plan.process(a, a)
         plan.status()
         assert np.all(vec == 0) and np.all(pk == -1), (ia, precision)
         plan.close()
+
+
+@pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
+def test_tc48_row_alignments(mode, orc):
+    """48 px windows on 512^2 crops of the 8- and 16-bit pairs at steps 8,
+    12, 10 and 9, whose window rows start on multiples of 8, 4, 2 and 1
+    pixels (the kernel's row loads follow): planes of split BF16 and the FP16
+    data split against numpy's FP64 correlation, exact pedestals, vectors
+    against the reference's peak search and fit on FP64 planes (peaks equal
+    but for near-ties, `assert_near_ties`)."""
+    pairs = {"u8": synth.config1(), "u16": synth.config2(size=1024)}
+    for name, (a, b) in pairs.items():
+        a, b = np.ascontiguousarray(a[:512, :512]), np.ascontiguousarray(b[:512, :512])
+        for step in (8, 12, 10, 9):
+            ref = fp64_reference(a, b, step, 48, mode, orc)
+            for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16):
+                got = run(a, b, step, precision, mode=mode, planes=True, ia=48)
+                assert np.array_equal(got["grid"], ref["grid"])
+                planes, ped = reference_planes(a, b, got["grid"], 48, mode)
+                assert np.array_equal(got["ped"], ped), (name, step, precision)
+                rtol = GENERIC_PLANE_RTOL[precision]
+                err = np.abs(got["planes"] - planes).max(axis=(1, 2)) / np.abs(planes).max(axis=(1, 2))
+                assert err.max() <= rtol, (name, step, precision, err.max())
+                assert_near_ties(got, ref, planes, rtol, (name, step, precision))
+                rms, mx, mm = displacement_error(got, ref)
+                rms_t, max_t, _ = BOUNDS[precision]
+                assert rms <= rms_t and mx <= max_t, (name, step, precision, rms, mx, mm)
 
 
 @pytest.mark.parametrize("mode", [og.CORR_COMPLEX, og.CORR_REAL])
@@ -360,6 +410,31 @@ def test_generic_kernel_64px_unaligned_grid(mode):
         rms, mx, mm = displacement_error(got, ref)
         rms_t, max_t, mm_t = BOUNDS[precision]
         assert rms <= rms_t and mx <= max_t and mm <= mm_t, (precision, rms, mx, mm)
+
+
+def test_limited_search_48px(orc):
+    """The limited peak search of the 48 px kernel against FP64 planes
+    through the reference's peak search on the central view (peaks equal
+    but for near-ties); the recipe itself checked first against the FP64
+    pass at 64 px."""
+    a, b = synth.config2(size=1024)
+    a, b = np.ascontiguousarray(a[:512, :512]), np.ascontiguousarray(b[:512, :512])
+    fp64_pass = run(a, b, 16, og.PREC_FP64, limit=True, ia=64)
+    recipe = fp64_reference(a, b, 16, 64, og.CORR_COMPLEX, orc, limit=True)
+    assert np.array_equal(recipe["peak"], fp64_pass["peak"])
+    rms, mx, mm = displacement_error(recipe, fp64_pass)
+    assert mx <= 1e-6 and mm == 0, (rms, mx, mm)
+    for step in (8, 12):
+        ref = fp64_reference(a, b, step, 48, og.CORR_COMPLEX, orc, limit=True)
+        planes = None
+        for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT2_FP16):
+            got = run(a, b, step, precision, limit=True, ia=48)
+            if planes is None:
+                planes, _ = reference_planes(a, b, got["grid"], 48)
+            assert_near_ties(got, ref, planes, GENERIC_PLANE_RTOL[precision], (step, precision))
+            rms, mx, mm = displacement_error(got, ref)
+            rms_t, max_t, _ = BOUNDS[precision]
+            assert rms <= rms_t and mx <= max_t, (step, precision, rms, mx, mm)
 
 
 def test_generic_limited_search_and_errors():
