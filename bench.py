@@ -779,7 +779,9 @@ def fp64_numpy_pass(a, b, grid, ia, img_h, chunk=2048):
 
 
 def run_sweep(args):
-    print(json.dumps(sweep_line(args.sweep_size)), flush=True)
+    sizes = tuple(int(w) for w in args.sweep_windows.split(","))
+    variants = tuple(args.sweep_variants.split(","))
+    print(json.dumps(sweep_line(args.sweep_size, variants=variants, sizes=sizes)), flush=True)
 
 
 def sweep_line(size, variants=("base", "sparse", "noisy"), sizes=(16, 32, 48, 64)):
@@ -1017,6 +1019,10 @@ def main():
     ap.add_argument("--mc-seeds", type=int, default=1000, help="Monte Carlo seeds of the adjoint workload")
     ap.add_argument("--sweep-size", type=int, default=2048,
                     help="image size of the precision sweep")
+    ap.add_argument("--sweep-windows", default="16,32,48,64",
+                    help="window sizes of the precision sweep (comma-separated)")
+    ap.add_argument("--sweep-variants", default="base,sparse,noisy",
+                    help="field variants of the precision sweep (comma-separated)")
     ap.add_argument("--no-other-workloads", action="store_true",
                     help="pair workload: skip the compact batch / sweep / adjoint records")
     ap.add_argument("--reference-seconds", type=float, default=120.0,

@@ -154,7 +154,8 @@ int opiv_plan_last_timing(opiv_plan* plan, float* fp32_ms, float* exact_ms);
  *   lie within the rounding may pick the other peak).  Needs u8/u16 frames
  *   and 16-byte aligned rows; 32 px windows also window x positions and x
  *   step multiples of 8 pixels; OPIV_ERR_UNSUPPORTED otherwise.  48 px windows need a plan from
- *   opiv_plan_create_tc (the FFT path takes powers of 2 only).  16 px grids
+ *   opiv_plan_create_tc (the FFT path takes powers of 2 only) and run a
+ *   kernel with one window per tile on any regular grid.  16 px grids
  *   with row steps of 1..6 pixels and window x positions and x step on
  *   multiples of 4 pixels run a kernel that stacks eight windows of a grid
  *   column per tile (each image row transformed once); other 16 px grids a

@@ -1,8 +1,9 @@
 // Host side of the tensor-core kernels (piv_tc_kernel.cuh for 32 px
 // windows, piv_tc16_kernel.cuh, piv_tc48_kernel.cuh and piv_tc64_kernel.cuh
-// for 16, 48 and 64 px grids they take, piv_tcg_kernel.cuh for the rest):
-// the constant matrices in BF16 and FP16 (hi and lo parts, canonical operand
-// layout) and the dispatch to the instantiation units.
+// for 16, 48 and 64 px grids they take, piv_tcg_kernel.cuh for the other
+// 16 and 64 px grids): the constant matrices in BF16 and FP16 (hi and lo
+// parts, canonical operand layout) and the dispatch to the instantiation
+// units.
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -34,8 +35,6 @@ cudaError_t launch_piv_tc16_bf16(const PivParams& p, int dtype, int mode, int li
 cudaError_t launch_piv_tc16_fp16(const PivParams& p, int dtype, int mode, int limit, int passes,
                                  const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tcg_w16(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
-                               const void* consts, cudaStream_t s);
-cudaError_t launch_piv_tcg_w48(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s);
 cudaError_t launch_piv_tcg_w64(const PivParams& p, int dtype, int mode, int limit, int passes, bool fp16,
                                const void* consts, cudaStream_t s);
@@ -175,11 +174,10 @@ cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int li
         return launch_piv_tcg_w16(p, dtype, mode, limit, passes, fp16, set, s);
     case 32: return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, set, s)
                          : launch_piv_tc_bf16(p, dtype, mode, limit, split, set, s);
-    case 48:   // grids at x multiples of 8: one window per tile
-        if (tc48_takes(p))
-            return fp16 ? launch_piv_tc48_fp16(p, dtype, mode, limit, passes, set, s)
-                        : launch_piv_tc48_bf16(p, dtype, mode, limit, split, set, s);
-        return launch_piv_tcg_w48(p, dtype, mode, limit, passes, fp16, set, s);
+    case 48:   // every regular grid: one window per tile (48 px plans take no window offsetting)
+        if (!tc48_takes(p)) return cudaErrorNotSupported;
+        return fp16 ? launch_piv_tc48_fp16(p, dtype, mode, limit, passes, set, s)
+                    : launch_piv_tc48_bf16(p, dtype, mode, limit, split, set, s);
     case 64:   // grids at x multiples of 8: one window per tile
         if (tc64_takes(p))
             return fp16 ? launch_piv_tc64_fp16(p, dtype, mode, limit, passes, set, s)

@@ -1,9 +1,9 @@
-// Tensor-core (tcgen05) PIV window path for 16, 48 and 64 px windows: the
-// same chain of four DFT matrix products as the 32 px kernel
-// (piv_tc_kernel.cuh), written once for any window size W that is a
-// multiple of 16 (a DFT matrix needs no power of two), without that
-// kernel's 32 px specialisations.  Instantiated per size in
-// piv_tcg_w16.cu, piv_tcg_w48.cu and piv_tcg_w64.cu.
+// Tensor-core (tcgen05) PIV window path for 16 and 64 px windows on the
+// grids that the dedicated kernels do not take: the same chain of four DFT
+// matrix products as the 32 px kernel (piv_tc_kernel.cuh), written once for
+// any window size W that is a multiple of 16 (a DFT matrix needs no power
+// of two), without that kernel's 32 px specialisations.  Instantiated per
+// size in piv_tcg_w16.cu and piv_tcg_w64.cu.
 //
 // Mathematics (a, b: the two windows, rows y, columns x, H = W / 2; all
 // transforms unnormalised like FFT::cross_correlate, fft.h:188-206):
@@ -23,8 +23,8 @@
 // Then find_peaks(plane, 2, 1) (image_utils.impl.h:42-74), the 3-point
 // Gaussian fit (impl:77-101) and the vector (main.cpp:220-236).
 //
-// A CTA of 4 warps takes tiles of 128 / W windows of one grid row (two for
-// W = 48).  Operands: shared memory, no-swizzle canonical layouts, hi and
+// A CTA of 4 warps takes tiles of 128 / W windows of one grid row (eight
+// 16 px or two 64 px windows).  Operands: shared memory, no-swizzle canonical layouts, hi and
 // lo parts for split precision; accumulators in tensor memory.  Rows of
 // the first product's M tiles, the second's and the fourth's follow the
 // thread index; the third product has M = 64 (row r in lane
