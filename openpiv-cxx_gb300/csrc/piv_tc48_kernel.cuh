@@ -132,45 +132,56 @@ __device__ __forceinline__ void tmem_ld16x2_24(uint32_t taddr, float* v)
     for (int i = 0; i < 24; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// 8 pixels of a row as one raw word for widen8 (pixel 0 in the low bytes),
-// loaded in words of al pixels (8, 4, 2 or 1: the alignment of the row start)
-template <typename PixT>
-__device__ __forceinline__ typename Raw<PixT>::type load8(const PixT* row, int al)
+// The 48 pixels of a window row as six raw 8-pixel words for widen8 (pixel
+// 0 in the low bytes), from the aligned 16-byte blocks that cover the row.
+// b, the row start's byte offset in its block, is the same for every row of
+// a window and both frames (frames 16-byte aligned, pitch a multiple of 16:
+// the host refuses other tensor-core passes), so the word select is uniform
+// over the group; the last block read is the one holding the row's last
+// pixel.
+template <typename PixT, int S>
+__device__ __forceinline__ void select_row48(const uint32_t* w, int sh, typename Raw<PixT>::type* raw)
 {
-    if (al == 8) return tc::load_raw<PixT>(row);
-    if constexpr (sizeof(PixT) == 2) {
-        if (al == 4) {
-            const uint2* q = reinterpret_cast<const uint2*>(row);
-            const uint2 a = __ldg(q), b = __ldg(q + 1);
-            return make_uint4(a.x, a.y, b.x, b.y);
-        }
-        if (al == 2) {
-            const unsigned int* q = reinterpret_cast<const unsigned int*>(row);
-            return make_uint4(__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3));
-        }
-        const unsigned short* q = reinterpret_cast<const unsigned short*>(row);
-        uint32_t w[4];
+    constexpr int NW = 12 * (int)sizeof(PixT);   // 32-bit words of a 48-pixel row
+    uint32_t o[NW];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) w[j] = (uint32_t)__ldg(q + 2 * j) | ((uint32_t)__ldg(q + 2 * j + 1) << 16);
-        return make_uint4(w[0], w[1], w[2], w[3]);
-    } else {
-        if (al == 4) {
-            const unsigned int* q = reinterpret_cast<const unsigned int*>(row);
-            return make_uint2(__ldg(q), __ldg(q + 1));
-        }
-        uint32_t w[2];
-        if (al == 2) {
-            const unsigned short* q = reinterpret_cast<const unsigned short*>(row);
+    for (int j = 0; j < NW; ++j) o[j] = __funnelshift_r(w[S + j], w[S + j + 1], sh);
 #pragma unroll
-            for (int j = 0; j < 2; ++j) w[j] = (uint32_t)__ldg(q + 2 * j) | ((uint32_t)__ldg(q + 2 * j + 1) << 16);
-        } else {
-            const unsigned char* q = reinterpret_cast<const unsigned char*>(row);
+    for (int g = 0; g < 6; ++g) {
+        if constexpr (sizeof(PixT) == 2) raw[g] = make_uint4(o[4 * g], o[4 * g + 1], o[4 * g + 2], o[4 * g + 3]);
+        else raw[g] = make_uint2(o[2 * g], o[2 * g + 1]);
+    }
+}
+
+template <typename PixT>
+__device__ __forceinline__ void load_row48(const PixT* row, typename Raw<PixT>::type* raw)
+{
+    constexpr int NB = 3 * (int)sizeof(PixT) + 1;   // blocks covering a row at any offset: 7 or 4
+    const uintptr_t a = reinterpret_cast<uintptr_t>(row);
+    const int b = (int)(a & 15u);
+    const uint4* blk = reinterpret_cast<const uint4*>(a - (uintptr_t)b);
+    uint32_t w[4 * NB];
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
-                w[j] = (uint32_t)__ldg(q + 4 * j) | ((uint32_t)__ldg(q + 4 * j + 1) << 8) |
-                       ((uint32_t)__ldg(q + 4 * j + 2) << 16) | ((uint32_t)__ldg(q + 4 * j + 3) << 24);
-        }
-        return make_uint2(w[0], w[1]);
+    for (int k = 0; k < NB - 1; ++k) {
+        const uint4 q = __ldg(blk + k);
+        w[4 * k] = q.x;
+        w[4 * k + 1] = q.y;
+        w[4 * k + 2] = q.z;
+        w[4 * k + 3] = q.w;
+    }
+    // the row reaches into one more block only when it does not start on one
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    if (b != 0) q = __ldg(blk + NB - 1);
+    w[4 * NB - 4] = q.x;
+    w[4 * NB - 3] = q.y;
+    w[4 * NB - 2] = q.z;
+    w[4 * NB - 1] = q.w;
+    const int sh = 8 * (b & 3);
+    switch (b >> 2) {
+    case 0: select_row48<PixT, 0>(w, sh, raw); break;
+    case 1: select_row48<PixT, 1>(w, sh, raw); break;
+    case 2: select_row48<PixT, 2>(w, sh, raw); break;
+    default: select_row48<PixT, 3>(w, sh, raw); break;
     }
 }
 
@@ -323,14 +334,6 @@ piv_tc48_kernel(const PivParams p, const uint4* __restrict__ consts)
     const PixT* fa = reinterpret_cast<const PixT*>(p.fa);
     const PixT* fb = reinterpret_cast<const PixT*>(p.fb);
     const size_t pitch = p.pitch / sizeof(PixT);
-    // the row loads' word: the widest of 8, 4, 2, 1 pixels on which every
-    // window row starts (grid origin and step, pitch, frame addresses)
-    auto aligned = [&](int a) {
-        const size_t bytes = (size_t)a * sizeof(PixT);
-        return p.gx0 % a == 0 && p.gdx % a == 0 && p.pitch % bytes == 0 &&
-               reinterpret_cast<uintptr_t>(p.fa) % bytes == 0 && reinterpret_cast<uintptr_t>(p.fb) % bytes == 0;
-    };
-    const int al = aligned(8) ? 8 : aligned(4) ? 4 : aligned(2) ? 2 : 1;
     // windows in grid order, each group a contiguous range
     const int64_t n_win = p.n_win;
     const int64_t vb = (int64_t)blockIdx.x * kGroups + grp, vg = (int64_t)gridDim.x * kGroups;
@@ -360,11 +363,12 @@ piv_tc48_kernel(const PivParams p, const uint4* __restrict__ consts)
             const float sg = ((f && (y & 1)) ? -1.f : 1.f) * kPix;
             uint32_t hw[24], lw[24];
             if (y < W) {
-                const PixT* row = (f ? fb : fa) + (size_t)(oy + y) * pitch + ox;
+                typename Raw<PixT>::type raw[6];
+                load_row48<PixT>((f ? fb : fa) + (size_t)(oy + y) * pitch + ox, raw);
 #pragma unroll
                 for (int g = 0; g < 6; ++g) {
                     float px[8];
-                    widen8<PixT>(load8<PixT>(row + 8 * g, al), px, sg);
+                    widen8<PixT>(raw[g], px, sg);
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         hw[4 * g + j] = pack2<F16>(px[2 * j], px[2 * j + 1]);
