@@ -1,11 +1,13 @@
 // Tensor-core (tcgen05) PIV window path for 48 x 48 windows, one window per
 // tile, BF16 or FP16 operands, split or plain (kernel templates; instantiated
-// in piv_tc48.cu and piv_tc48_fp16.cu): the 64 px kernel's design (piv_tc64_kernel.cuh) at
-// W = 48, H = 24 -- the 2-D cross-correlation of every window pair as four
-// chained DFT matrix products (FFT::cross_correlate, fft.h:188-206, without
-// its power-of-two restriction: a DFT matrix needs none), then
-// find_peaks(plane, 2, 1), the 3-point Gaussian fit and the vector
-// (image_utils.impl.h:42-101, main.cpp:214-236).
+// in piv_tc48.cu and piv_tc48_fp16.cu): the 64 px kernel's design
+// (piv_tc64_kernel.cuh) at W = 48, H = 24 -- the 2-D cross-correlation of
+// every window pair as four chained DFT matrix products
+// (FFT::cross_correlate, fft.h:188-206, without its power-of-two
+// restriction: a DFT matrix needs none), then find_peaks(plane, 2, 1), the
+// 3-point Gaussian fit and the vector (image_utils.impl.h:42-101,
+// main.cpp:214-236).  Any regular grid: a window row loads from the 16-byte
+// blocks that cover it (load_row48).
 //
 // One CTA per SM runs kGroups independent tile groups of 4 warps sharing one
 // copy of the constants; a group takes one window at a time, has 128
