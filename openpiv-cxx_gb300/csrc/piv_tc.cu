@@ -174,7 +174,7 @@ cudaError_t launch_piv_tc(const PivParams& p, int w, int dtype, int mode, int li
         return launch_piv_tcg_w16(p, dtype, mode, limit, passes, fp16, set, s);
     case 32: return fp16 ? launch_piv_tc_fp16(p, dtype, mode, limit, split, set, s)
                          : launch_piv_tc_bf16(p, dtype, mode, limit, split, set, s);
-    case 48:   // every regular grid: one window per tile (48 px plans take no window offsetting)
+    case 48:   // every regular grid: one window per tile
         if (!tc48_takes(p)) return cudaErrorNotSupported;
         return fp16 ? launch_piv_tc48_fp16(p, dtype, mode, limit, passes, set, s)
                     : launch_piv_tc48_bf16(p, dtype, mode, limit, split, set, s);

@@ -799,8 +799,8 @@ piv_tc48_kernel(const PivParams p, const uint4* __restrict__ consts)
     if (threadIdx.x < 32) tcx::tmem_dealloc(tcta, kGroups * kGroupCols);
 }
 
-// any regular grid (the row loads follow its alignment); per-window
-// positions and window offsetting run the generic kernel
+// every regular grid; per-window positions and window offsetting are not
+// tensor-core features (the exact pass and the FP32 multi-pass chains)
 inline bool applicable(const PivParams& p) { return p.win_xy == nullptr && p.prev_disp == nullptr; }
 
 template <bool F16, bool SPLIT, bool CSPLIT, int MODE, bool LIMIT, typename PixT>
