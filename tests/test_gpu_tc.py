@@ -1,6 +1,8 @@
-"""Tensor-core DFT-GEMM path (32 x 32 windows): correlation planes against
-numpy's FP64 FFT correlation, vectors against the FP64 pass (the
-reference's arithmetic on every window), argument errors."""
+"""Tensor-core DFT-GEMM path (16, 32, 48 and 64 px windows): correlation
+planes against numpy's FP64 FFT correlation, vectors against the FP64 pass
+(the reference's arithmetic on every window; for 48 px, which the
+reference's FFT rejects, FP64 planes through its peak search and fit),
+argument errors."""
 import numpy as np
 import pytest
 
@@ -177,6 +179,24 @@ def test_full_range_uint16(ia, step):
         assert err.max() <= 5 * SPLIT_PLANE_RTOL, f"plane error {err.max():.3e} of the plane peak"
         rms, mx, mm = displacement_error(got, ref)
         assert rms <= SPLIT_RMS and mx <= SPLIT_MAX and mm <= SPLIT_MISMATCH, (precision, rms, mx, mm)
+
+
+def test_full_range_uint16_48px(orc):
+    """48 px windows on full-range 16-bit frames (pixels to 65535): exact
+    pedestals, planes against numpy's FP64 correlation, vectors
+    against FP64 planes through the reference's peak search and fit (peaks
+    equal but for near-ties)."""
+    a, b = full_range_pair(512)
+    ref = fp64_reference(a, b, 12, 48, og.CORR_COMPLEX, orc)
+    for precision in (og.PREC_TC_SPLIT_BF16, og.PREC_TC_SPLIT_FP16):
+        got = run(a, b, 12, precision, planes=True, ia=48)
+        planes, ped = reference_planes(a, b, got["grid"], 48)
+        assert np.array_equal(got["ped"], ped), "pedestal not exact"
+        err = np.abs(got["planes"] - planes).max(axis=(1, 2)) / np.abs(planes).max(axis=(1, 2))
+        assert err.max() <= 5 * SPLIT_PLANE_RTOL, f"plane error {err.max():.3e} of the plane peak"
+        assert_near_ties(got, ref, planes, 5 * SPLIT_PLANE_RTOL, precision)
+        rms, mx, mm = displacement_error(got, ref)
+        assert rms <= SPLIT_RMS and mx <= SPLIT_MAX, (precision, rms, mx, mm)
 
 
 @pytest.mark.parametrize("step", [16, 8])
